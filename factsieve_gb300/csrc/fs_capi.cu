@@ -1,0 +1,693 @@
+// fs_capi.cu -- the C ABI of libfactsieve.so (declared in include/factsieve.h).
+//
+// Owns device memory, streams and the per-n setup plans, and sequences the
+// kernels of one p-segment the way the reference's cl_sieve() loop does
+// (cl_sieve.cpp:1107-1241): candidates -> (first segment) table check ->
+// setup -> iterate -> check.  Nothing here calls exit(); every failure is a
+// status code, and the text of the last CUDA error stays on the context.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/factsieve.h"
+#include "fs_host.h"
+#include "fs_launch.h"
+
+static_assert(sizeof(fs_factor) == 16, "factor record is 16 bytes");
+static_assert(sizeof(fs_factor) == sizeof(fs::Factor), "factor layouts agree");
+static_assert(sizeof(fs_counters) == sizeof(fs::Counters), "counter layouts agree");
+
+namespace {
+
+constexpr u32 kQ[29] = {3,  5,  7,  11, 13, 17, 19, 23, 29,  31,  37,  41,  43,  47, 53,
+                        59, 61, 67, 71, 73, 79, 83, 89, 97, 101, 103, 107, 109, 113};
+
+struct PlanGPU {
+    uint32_t n = 0, nchunks = 0;
+    u64* d_words = nullptr;
+    fs::Layer* d_layers = nullptr;
+    fs::PlanChunkDev* d_chunks = nullptr;
+    uint64_t deficit = 0, nwords = 0;
+    uint32_t nlayers = 0;
+    std::vector<fs::PlanChunkDev> chunks;
+};
+
+}  // namespace
+
+struct fs_ctx {
+    int device = 0;
+    cudaStream_t own = nullptr, stream = nullptr;
+    int sm_count = 0, clock_khz = 0;
+    uint64_t total_mem = 0;
+    int sieve_occ = 1;
+    fs_tuning tuning{};
+    std::string err;
+    // search state
+    bool active = false, table_checked = false;
+    uint64_t pmin = 0, pmax = 0;
+    uint32_t nmin = 0, nmax = 0;
+    fs::Counters* d_ctr = nullptr;
+    u64* d_cand = nullptr;
+    uint64_t cand_cap = 0;
+    u64* d_residue = nullptr;
+    uint64_t residue_cap = 0;
+    u64* d_partials = nullptr;
+    uint64_t partials_cap = 0;
+    fs::Factor* d_hits = nullptr;
+    uint32_t hit_cap = 0;
+    u64* d_chk_scratch = nullptr;
+    u32* d_chk_done = nullptr;
+    u64* d_chk_result = nullptr;
+    int chk_grid = 0;
+    u32* d_sink = nullptr;
+    std::map<std::pair<uint32_t, uint32_t>, PlanGPU> plans;
+};
+
+#define CK(ctx, call)                                                          \
+    do {                                                                       \
+        cudaError_t e_ = (call);                                               \
+        if (e_ != cudaSuccess) {                                               \
+            (ctx)->err = std::string(#call) + ": " + cudaGetErrorString(e_);   \
+            return e_ == cudaErrorMemoryAllocation ? FS_E_NOMEM : FS_E_CUDA;   \
+        }                                                                      \
+    } while (0)
+
+namespace {
+
+int bind(fs_ctx* c) {
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e != cudaSuccess) {
+        c->err = std::string("cudaSetDevice: ") + cudaGetErrorString(e);
+        return FS_E_CUDA;
+    }
+    return FS_OK;
+}
+
+template <class T>
+int grow(fs_ctx* c, T** ptr, uint64_t* have, uint64_t need) {
+    if (*have >= need && *ptr) return FS_OK;
+    if (*ptr) {
+        CK(c, cudaStreamSynchronize(c->stream));
+        CK(c, cudaFree(*ptr));
+        *ptr = nullptr;
+        *have = 0;
+    }
+    CK(c, cudaMalloc((void**)ptr, need * sizeof(T)));
+    *have = need;
+    return FS_OK;
+}
+
+void free_plans(fs_ctx* c) {
+    for (auto& kv : c->plans) {
+        cudaFree(kv.second.d_words);
+        cudaFree(kv.second.d_layers);
+        cudaFree(kv.second.d_chunks);
+    }
+    c->plans.clear();
+}
+
+int get_plan(fs_ctx* c, uint32_t n, uint32_t chunks, PlanGPU** out) {
+    auto key = std::make_pair(n, chunks);
+    auto it = c->plans.find(key);
+    if (it != c->plans.end()) {
+        *out = &it->second;
+        return FS_OK;
+    }
+    fs::SetupPlan hp = fs::build_plan(n, chunks);
+    PlanGPU g;
+    g.n = n;
+    g.nchunks = chunks;
+    g.deficit = hp.deficit;
+    g.nwords = hp.words.size();
+    g.nlayers = (uint32_t)hp.layers.size();
+    for (auto& ch : hp.chunks) g.chunks.push_back({ch.layer_begin, ch.layer_end, ch.deficit});
+    // +2 words of padding keep the paired 16-byte loads inside the buffer
+    size_t wbytes = (hp.words.size() + 2) * sizeof(u64);
+    CK(c, cudaMalloc((void**)&g.d_words, wbytes));
+    CK(c, cudaMalloc((void**)&g.d_layers, (hp.layers.size() + 1) * sizeof(fs::Layer)));
+    CK(c, cudaMalloc((void**)&g.d_chunks, (g.chunks.size() + 1) * sizeof(fs::PlanChunkDev)));
+    CK(c, cudaMemsetAsync(g.d_words, 0, wbytes, c->stream));
+    if (!hp.words.empty())
+        CK(c, cudaMemcpyAsync(g.d_words, hp.words.data(), hp.words.size() * sizeof(u64),
+                              cudaMemcpyHostToDevice, c->stream));
+    if (!hp.layers.empty())
+        CK(c, cudaMemcpyAsync(g.d_layers, hp.layers.data(), hp.layers.size() * sizeof(fs::Layer),
+                              cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(g.d_chunks, g.chunks.data(), g.chunks.size() * sizeof(fs::PlanChunkDev),
+                          cudaMemcpyHostToDevice, c->stream));
+    // the host vectors die here: wait for the copies
+    CK(c, cudaStreamSynchronize(c->stream));
+    auto ins = c->plans.emplace(key, std::move(g));
+    *out = &ins.first->second;
+    return FS_OK;
+}
+
+fs::SieveArgs base_args(PlanGPU* pl) {
+    fs::SieveArgs a;
+    memset(&a, 0, sizeof(a));
+    if (pl) {
+        a.plan.words = pl->d_words;
+        a.plan.layers = pl->d_layers;
+        a.plan.layer_begin = 0;
+        a.plan.layer_end = pl->nlayers;
+        a.plan.deficit = pl->deficit;
+        a.chunks = pl->d_chunks;
+        a.nchunks = pl->nchunks;
+    }
+    return a;
+}
+
+int sieve_grid(fs_ctx* c) {
+    int bpsm = c->tuning.sieve_blocks_per_sm ? (int)c->tuning.sieve_blocks_per_sm : c->sieve_occ;
+    return std::max(1, c->sm_count * bpsm);
+}
+
+// How many threads should share one prime's setup: enough to fill the GPU
+// when the candidates alone cannot, and only when the table is long.
+uint32_t auto_chunks(fs_ctx* c, uint64_t est_cand, uint32_t n) {
+    if (c->tuning.setup_chunks) return c->tuning.setup_chunks;
+    const uint64_t slots = (uint64_t)c->sm_count * 2048;
+    const double words = 0.03 * n;   // bit-layered table length, about 0.03 n words
+    if (words < 8192 || est_cand * 2 >= slots) return 1;
+    uint64_t k = slots / std::max<uint64_t>(est_cand, 1);
+    k = std::min<uint64_t>(k, (uint64_t)(words / 2048));
+    return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(k, 64));
+}
+
+int run_gen(fs_ctx* c, uint64_t low, uint64_t high, u64* d_cand, uint32_t cap, fs::Counters* d_ctr) {
+    if (high <= low) return FS_OK;
+    uint64_t o0 = low | 1ull;
+    if (o0 < low || o0 >= high) return FS_OK;
+    fs::GenArgs g;
+    memset(&g, 0, sizeof(g));
+    g.o0 = o0;
+    g.high = high;
+    g.nwords = (high - o0 + 63) / 64;
+    if (g.nwords >= (1ull << 31)) {
+        c->err = "segment too wide for one candidate launch";
+        return FS_E_ARG;
+    }
+    for (int j = 0; j < 29; ++j) g.r0[j] = (u32)(o0 % kQ[j]);
+    g.cap = cap;
+    g.cand = d_cand;
+    g.ctr = d_ctr;
+    const int threads = fs::gen_threads();
+    uint64_t blocks = (g.nwords + threads - 1) / threads;
+    uint64_t maxb = (uint64_t)c->sm_count * (c->tuning.gen_blocks_per_sm ? c->tuning.gen_blocks_per_sm : 8);
+    CK(c, fs::launch_gen(g, (int)std::max<uint64_t>(1, std::min(blocks, maxb)), c->stream));
+    return FS_OK;
+}
+
+int run_table_check(fs_ctx* c, const u64* d_cand, fs::Counters* d_ctr, uint32_t n, PlanGPU* pl) {
+    if (!c->d_chk_scratch) {
+        c->chk_grid = c->sm_count * 4;
+        CK(c, cudaMalloc((void**)&c->d_chk_scratch, c->chk_grid * sizeof(u64)));
+        CK(c, cudaMalloc((void**)&c->d_chk_done, sizeof(u32)));
+        CK(c, cudaMalloc((void**)&c->d_chk_result, 2 * sizeof(u64)));
+        CK(c, cudaMemsetAsync(c->d_chk_done, 0, sizeof(u32), c->stream));
+    }
+    fs::TableCheckArgs t;
+    memset(&t, 0, sizeof(t));
+    t.cand = d_cand;
+    t.ncand = &d_ctr->ncand;
+    t.n0 = n;
+    t.words = pl->d_words;
+    t.layers = pl->d_layers;
+    t.chunks = pl->d_chunks;
+    t.nchunks = pl->nchunks;
+    t.deficit = pl->deficit;
+    t.scratch = c->d_chk_scratch;
+    t.done = c->d_chk_done;
+    t.result = c->d_chk_result;
+    t.ctr = d_ctr;
+    CK(c, cudaMemsetAsync(c->d_chk_result, 0, 2 * sizeof(u64), c->stream));
+    CK(c, fs::launch_table_check(t, c->chk_grid, c->stream));
+    return FS_OK;
+}
+
+// setup + iterate + check of the candidates in d_cand over [nstart, nend),
+// finishing with s7 = nmax R when final.  Splits the n-range into launches
+// of at most tuning.max_steps_per_launch steps, and the table across
+// threads when auto_chunks() says so.
+int run_sieve(fs_ctx* c, const u64* d_cand, uint32_t cap, fs::Counters* d_ctr, uint32_t nstart,
+              uint32_t nend, uint32_t nmax, bool count, uint64_t est_cand, fs::Factor* d_hits,
+              uint32_t hitcap) {
+    uint32_t chunks = auto_chunks(c, est_cand, nstart);
+    PlanGPU* pl = nullptr;
+    int rc = get_plan(c, nstart, chunks, &pl);
+    if (rc) return rc;
+    const uint32_t span = nend > nstart ? nend - nstart : 0;
+    const uint32_t maxs = c->tuning.max_steps_per_launch;
+    const bool split = maxs && span > maxs;
+    if (split) {
+        if ((rc = grow(c, &c->d_residue, &c->residue_cap, (uint64_t)cap + 1))) return rc;
+    }
+    const int grid = sieve_grid(c);
+    fs::SieveArgs a = base_args(pl);
+    a.cand = d_cand;
+    a.ncand = &d_ctr->ncand;
+    a.cap = cap;
+    a.hits = d_hits;
+    a.hitcap = hitcap;
+    a.ctr = d_ctr;
+    a.nmax = nmax;
+    int setup_mode = fs::SETUP_PLAN;
+    if (chunks > 1) {
+        if ((rc = grow(c, &c->d_partials, &c->partials_cap, (uint64_t)cap * chunks + 1))) return rc;
+        a.partials = c->d_partials;
+        int gx = std::max(1, sieve_grid(c) / (int)chunks);
+        CK(c, fs::launch_setup_partial(a, gx, (int)chunks, c->stream));
+        setup_mode = fs::SETUP_PARTIALS;
+    }
+    uint32_t s = nstart;
+    bool first = true;
+    do {
+        uint32_t e = split ? std::min<uint64_t>((uint64_t)s + maxs, nend) : nend;
+        const bool fin = (e == nend);
+        a.nstart = s;
+        a.nend = e;
+        a.residue = split ? c->d_residue : nullptr;
+        a.count_candidates = (fin && count) ? 1u : 0u;
+        a.store_final = 0;
+        CK(c, fs::launch_sieve(a, first ? setup_mode : fs::SETUP_LOAD, fin, grid, c->stream));
+        first = false;
+        s = e;
+    } while (s < nend);
+    return FS_OK;
+}
+
+uint64_t est_candidates(uint64_t low, uint64_t high) {
+    if (high <= low) return 0;
+    double w = (double)(high - low);
+    double lx = std::log(std::max<double>((double)low, 3.0));
+    return (uint64_t)(w / lx * 1.05) + 16;
+}
+
+}  // namespace
+
+// =================================================================== ABI ===
+
+extern "C" {
+
+int fs_version(void) { return 10000; }
+
+const char* fs_strerror(int code) {
+    switch (code) {
+        case FS_OK: return "ok";
+        case FS_E_ARG: return "invalid argument";
+        case FS_E_CUDA: return "CUDA error";
+        case FS_E_OVERFLOW: return "candidate or factor buffer overflow";
+        case FS_E_VALIDATION: return "gpu validation failure";
+        case FS_E_TABLE: return "power table verification failed";
+        case FS_E_NOMEM: return "out of memory";
+        case FS_E_VERIFY: return "CPU factor verification failed";
+        case FS_E_STATE: return "call out of order";
+        case FS_E_TIMEOUT: return "timed out";
+        default: return "unknown error";
+    }
+}
+
+const char* fs_last_error(fs_ctx* ctx) { return ctx ? ctx->err.c_str() : ""; }
+
+int fs_device_count(int* count) {
+    if (!count) return FS_E_ARG;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) {
+        *count = 0;
+        return FS_E_CUDA;
+    }
+    *count = n;
+    return FS_OK;
+}
+
+int fs_create(int device, fs_ctx** out) {
+    if (!out) return FS_E_ARG;
+    *out = nullptr;
+    fs_ctx* c = new fs_ctx();
+    c->device = device;
+    int rc = bind(c);
+    if (rc) {
+        delete c;
+        return rc;
+    }
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return FS_E_CUDA;
+    }
+    c->stream = c->own;
+    c->sm_count = prop.multiProcessorCount;
+    int clk = 0;
+    cudaDeviceGetAttribute(&clk, cudaDevAttrClockRate, device);
+    c->clock_khz = clk;
+    c->total_mem = prop.totalGlobalMem;
+    int occ = 0;
+    if (fs::sieve_occupancy(&occ) == cudaSuccess && occ > 0) c->sieve_occ = occ;
+    if (cudaMalloc((void**)&c->d_ctr, sizeof(fs::Counters)) != cudaSuccess ||
+        cudaMalloc((void**)&c->d_sink, 4096 * sizeof(u32)) != cudaSuccess) {
+        cudaStreamDestroy(c->own);
+        delete c;
+        return FS_E_NOMEM;
+    }
+    cudaMemset(c->d_ctr, 0, sizeof(fs::Counters));
+    *out = c;
+    return FS_OK;
+}
+
+int fs_destroy(fs_ctx* c) {
+    if (!c) return FS_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    free_plans(c);
+    cudaFree(c->d_ctr);
+    cudaFree(c->d_cand);
+    cudaFree(c->d_residue);
+    cudaFree(c->d_partials);
+    cudaFree(c->d_hits);
+    cudaFree(c->d_chk_scratch);
+    cudaFree(c->d_chk_done);
+    cudaFree(c->d_chk_result);
+    cudaFree(c->d_sink);
+    if (c->own) cudaStreamDestroy(c->own);
+    delete c;
+    return FS_OK;
+}
+
+int fs_set_stream(fs_ctx* c, void* stream) {
+    if (!c) return FS_E_ARG;
+    c->stream = stream ? (cudaStream_t)stream : c->own;
+    return FS_OK;
+}
+
+void* fs_get_stream(fs_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int fs_set_tuning(fs_ctx* c, const fs_tuning* t) {
+    if (!c || !t) return FS_E_ARG;
+    c->tuning = *t;
+    return FS_OK;
+}
+
+int fs_get_tuning(fs_ctx* c, fs_tuning* t) {
+    if (!c || !t) return FS_E_ARG;
+    *t = c->tuning;
+    if (!t->sieve_blocks_per_sm) t->sieve_blocks_per_sm = (uint32_t)c->sieve_occ;
+    return FS_OK;
+}
+
+int fs_device_info(fs_ctx* c, int* sm_count, int* clock_khz, uint64_t* total_mem) {
+    if (!c) return FS_E_ARG;
+    if (sm_count) *sm_count = c->sm_count;
+    if (clock_khz) *clock_khz = c->clock_khz;
+    if (total_mem) *total_mem = c->total_mem;
+    return FS_OK;
+}
+
+int fs_synchronize(fs_ctx* c) {
+    if (!c) return FS_E_ARG;
+    int rc = bind(c);
+    if (rc) return rc;
+    CK(c, cudaStreamSynchronize(c->stream));
+    return FS_OK;
+}
+
+uint64_t fs_candidate_capacity(uint64_t low, uint64_t high) {
+    if (high <= low) return 1024;
+    const double w = (double)(high - low);
+    // Brun-Titchmarsh in the Montgomery-Vaughan form: an interval of length
+    // w > 1 holds at most 2w/ln w primes; base-2 strong pseudoprimes with no
+    // factor <= 113 are far rarer than the 1024-slot margin.
+    double bound = w > 2.0 ? 2.0 * w / std::log(w) : w + 1;
+    double wheel = 8.0 * std::ceil(w / 30.0) + 16;   // numbers coprime to 30
+    double cap = std::min(bound, wheel) * 1.02 + 1024;
+    return (uint64_t)std::min(cap, 4.0e9);
+}
+
+int fs_search_begin(fs_ctx* c, uint64_t pmin, uint64_t pmax, uint32_t nmin, uint32_t nmax,
+                    uint32_t result_cap) {
+    if (!c) return FS_E_ARG;
+    // setupSearch's checks (cl_sieve.cpp:561-589)
+    if (pmin == 0 || pmax == 0 || nmin == 0 || nmax == 0 || nmin > nmax || pmin > pmax || pmin < nmin) {
+        c->err = "invalid search range";
+        return FS_E_ARG;
+    }
+    int rc = bind(c);
+    if (rc) return rc;
+    c->pmin = pmin;
+    c->pmax = pmax;
+    c->nmin = nmin;
+    c->nmax = nmax;
+    c->active = true;
+    c->table_checked = false;
+    uint32_t cap = result_cap ? result_cap : (pmin < 0xFFFFFFFFull ? 30000000u : 1000000u);
+    uint64_t have = c->hit_cap;
+    if ((rc = grow(c, &c->d_hits, &have, cap))) return rc;
+    c->hit_cap = cap;
+    CK(c, cudaMemsetAsync(c->d_ctr, 0, sizeof(fs::Counters), c->stream));
+    return FS_OK;
+}
+
+int fs_search_segment(fs_ctx* c, uint64_t low, uint64_t high) {
+    if (!c) return FS_E_ARG;
+    if (!c->active) return FS_E_STATE;
+    int rc = bind(c);
+    if (rc) return rc;
+    if (high <= low) return FS_OK;
+    uint64_t cap64 = fs_candidate_capacity(low, high);
+    if (cap64 >= 0xFFFFFFF0ull) {
+        c->err = "segment too wide";
+        return FS_E_ARG;
+    }
+    const uint32_t cap = (uint32_t)cap64;
+    if ((rc = grow(c, &c->d_cand, &c->cand_cap, cap64))) return rc;
+    CK(c, cudaMemsetAsync(&c->d_ctr->ncand, 0, sizeof(u32), c->stream));
+    if ((rc = run_gen(c, low, high, c->d_cand, cap, c->d_ctr))) return rc;
+    if (!c->table_checked) {
+        PlanGPU* pl = nullptr;
+        if ((rc = get_plan(c, c->nmin, 1, &pl))) return rc;
+        if ((rc = run_table_check(c, c->d_cand, c->d_ctr, c->nmin, pl))) return rc;
+        c->table_checked = true;
+    }
+    return run_sieve(c, c->d_cand, cap, c->d_ctr, c->nmin, c->nmax, c->nmax, true,
+                     est_candidates(low, high), c->d_hits, c->hit_cap);
+}
+
+int fs_search_range(fs_ctx* c, uint64_t low, uint64_t high, uint64_t seg_width) {
+    if (!c) return FS_E_ARG;
+    if (!seg_width) seg_width = 1000000000ull;
+    for (uint64_t lo = low; lo < high;) {
+        uint64_t hi = lo + seg_width;
+        if (hi > high || hi < lo) hi = high;
+        int rc = fs_search_segment(c, lo, hi);
+        if (rc) return rc;
+        lo = hi;
+    }
+    return FS_OK;
+}
+
+int fs_search_collect(fs_ctx* c, fs_factor* out, uint64_t cap, uint64_t* nfactors, uint64_t* raw_sum,
+                      uint64_t* primecount, uint32_t* flags) {
+    if (!c) return FS_E_ARG;
+    if (!c->active) return FS_E_STATE;
+    int rc = bind(c);
+    if (rc) return rc;
+    fs::Counters h;
+    CK(c, cudaMemcpyAsync(&h, c->d_ctr, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    uint64_t nh = std::min<uint64_t>(h.nhits, c->hit_cap);
+    if (nfactors) *nfactors = h.nhits;
+    if (raw_sum) *raw_sum = h.raw_sum;
+    if (primecount) *primecount = h.primecount;
+    if (flags) *flags = h.flags;
+    uint64_t ncopy = std::min<uint64_t>(nh, out ? cap : 0);
+    if (ncopy)
+        CK(c, cudaMemcpy(out, c->d_hits, ncopy * sizeof(fs_factor), cudaMemcpyDeviceToHost));
+    // clear sums, hits and flags for the next interval (clearresult.cl)
+    CK(c, cudaMemsetAsync(c->d_ctr, 0, offsetof(fs::Counters, ncand), c->stream));
+    CK(c, cudaMemsetAsync(&c->d_ctr->nhits, 0, 2 * sizeof(u32), c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    if (h.flags & FS_FLAG_TABLE) return FS_E_TABLE;
+    if (h.flags & FS_FLAG_VALIDATION) return FS_E_VALIDATION;
+    if (h.flags & (FS_FLAG_CAND_OVERFLOW | FS_FLAG_HIT_OVERFLOW)) return FS_E_OVERFLOW;
+    if (h.nhits > c->hit_cap || (out && h.nhits > cap)) return FS_E_OVERFLOW;
+    return FS_OK;
+}
+
+// ------------------------------------------------------------ stage-level --
+
+int fs_getsegprimes(fs_ctx* c, uint64_t low, uint64_t high, uint64_t* d_cand, uint32_t cap,
+                    fs_counters* d_ctr) {
+    if (!c || !d_cand || !d_ctr) return FS_E_ARG;
+    int rc = bind(c);
+    if (rc) return rc;
+    return run_gen(c, low, high, (u64*)d_cand, cap, (fs::Counters*)d_ctr);
+}
+
+int fs_setup(fs_ctx* c, const uint64_t* d_cand, uint32_t cap, fs_counters* d_ctr, uint32_t nstart,
+             uint64_t* d_residue) {
+    if (!c || !d_cand || !d_ctr || !d_residue) return FS_E_ARG;
+    int rc = bind(c);
+    if (rc) return rc;
+    const uint32_t chunks = c->tuning.setup_chunks ? c->tuning.setup_chunks : 1;
+    PlanGPU* pl = nullptr;
+    if ((rc = get_plan(c, nstart, chunks, &pl))) return rc;
+    fs::SieveArgs a = base_args(pl);
+    a.cand = (const u64*)d_cand;
+    a.ncand = &((fs::Counters*)d_ctr)->ncand;
+    a.cap = cap;
+    a.ctr = (fs::Counters*)d_ctr;
+    a.residue = (u64*)d_residue;
+    a.nstart = a.nend = nstart;
+    int mode = fs::SETUP_PLAN;
+    if (chunks > 1) {
+        if ((rc = grow(c, &c->d_partials, &c->partials_cap, (uint64_t)cap * chunks + 1))) return rc;
+        a.partials = c->d_partials;
+        CK(c, fs::launch_setup_partial(a, std::max(1, sieve_grid(c) / (int)chunks), (int)chunks, c->stream));
+        mode = fs::SETUP_PARTIALS;
+    }
+    CK(c, fs::launch_sieve(a, mode, false, sieve_grid(c), c->stream));
+    return FS_OK;
+}
+
+int fs_iterate(fs_ctx* c, const uint64_t* d_cand, uint32_t cap, fs_counters* d_ctr, uint64_t* d_residue,
+               uint32_t nstart, uint32_t nend, fs_factor* d_hits, uint32_t hitcap) {
+    if (!c || !d_cand || !d_ctr || !d_residue || (!d_hits && hitcap)) return FS_E_ARG;
+    if (nend > 0x7FFFFFFFu) return FS_E_ARG;
+    int rc = bind(c);
+    if (rc) return rc;
+    fs::SieveArgs a = base_args(nullptr);
+    a.cand = (const u64*)d_cand;
+    a.ncand = &((fs::Counters*)d_ctr)->ncand;
+    a.cap = cap;
+    a.ctr = (fs::Counters*)d_ctr;
+    a.residue = (u64*)d_residue;
+    a.hits = (fs::Factor*)d_hits;
+    a.hitcap = hitcap;
+    const uint32_t maxs = c->tuning.max_steps_per_launch;
+    uint32_t s = nstart;
+    do {
+        uint32_t e = (maxs && nend - s > maxs) ? s + maxs : nend;
+        a.nstart = s;
+        a.nend = e;
+        CK(c, fs::launch_sieve(a, fs::SETUP_LOAD, false, sieve_grid(c), c->stream));
+        s = e;
+    } while (s < nend);
+    return FS_OK;
+}
+
+int fs_check(fs_ctx* c, const uint64_t* d_cand, uint32_t cap, fs_counters* d_ctr, const uint64_t* d_residue,
+             uint32_t nmax) {
+    if (!c || !d_cand || !d_ctr || !d_residue) return FS_E_ARG;
+    int rc = bind(c);
+    if (rc) return rc;
+    fs::SieveArgs a = base_args(nullptr);
+    a.cand = (const u64*)d_cand;
+    a.ncand = &((fs::Counters*)d_ctr)->ncand;
+    a.cap = cap;
+    a.ctr = (fs::Counters*)d_ctr;
+    a.residue = (u64*)d_residue;
+    a.nstart = a.nend = nmax;
+    a.nmax = nmax;
+    a.count_candidates = 1;
+    a.store_final = 0;
+    CK(c, fs::launch_sieve(a, fs::SETUP_LOAD, true, sieve_grid(c), c->stream));
+    return FS_OK;
+}
+
+int fs_table_check(fs_ctx* c, const uint64_t* d_cand, fs_counters* d_ctr, uint32_t nmin, uint64_t* out2) {
+    if (!c || !d_cand || !d_ctr) return FS_E_ARG;
+    int rc = bind(c);
+    if (rc) return rc;
+    const uint32_t chunks = c->tuning.setup_chunks ? c->tuning.setup_chunks : 1;
+    PlanGPU* pl = nullptr;
+    if ((rc = get_plan(c, nmin, chunks, &pl))) return rc;
+    if ((rc = run_table_check(c, (const u64*)d_cand, (fs::Counters*)d_ctr, nmin, pl))) return rc;
+    if (out2) {
+        CK(c, cudaMemcpyAsync(out2, c->d_chk_result, 2 * sizeof(u64), cudaMemcpyDeviceToHost, c->stream));
+        CK(c, cudaStreamSynchronize(c->stream));
+    }
+    return FS_OK;
+}
+
+int fs_bench_int_pipe(fs_ctx* c, uint32_t kind, uint32_t iters, double* ops_per_sec, double* ms) {
+    if (!c || kind > 3) return FS_E_ARG;
+    int rc = bind(c);
+    if (rc) return rc;
+    const int grid = c->sm_count * 8;   // 8 x 256 threads = 2048 per SM
+    cudaEvent_t e0, e1;
+    CK(c, cudaEventCreate(&e0));
+    CK(c, cudaEventCreate(&e1));
+    CK(c, fs::launch_imad_bench(iters / 8 + 1, kind, 12345, c->d_sink, grid, c->stream));   // warm-up
+    CK(c, cudaEventRecord(e0, c->stream));
+    CK(c, fs::launch_imad_bench(iters, kind, 12345, c->d_sink, grid, c->stream));
+    CK(c, cudaEventRecord(e1, c->stream));
+    CK(c, cudaEventSynchronize(e1));
+    float t = 0;
+    CK(c, cudaEventElapsedTime(&t, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    const double ops = (double)grid * 256.0 * (double)iters * 8.0;
+    if (ms) *ms = t;
+    if (ops_per_sec) *ops_per_sec = t > 0 ? ops / (t * 1e-3) : 0;
+    return FS_OK;
+}
+
+// ---------------------------------------------------------------- host ----
+
+int fs_power_table(uint32_t n, uint64_t* prime, uint32_t* exp, uint32_t* bit, uint32_t cap, uint32_t* len) {
+    fs::RefTable t = fs::reference_table(n);
+    if (len) *len = (uint32_t)t.prime.size();
+    if (t.prime.size() > cap) return FS_E_OVERFLOW;
+    for (size_t i = 0; i < t.prime.size(); ++i) {
+        if (prime) prime[i] = t.prime[i];
+        if (exp) exp[i] = t.exp[i];
+        if (bit) bit[i] = t.bit[i];
+    }
+    return FS_OK;
+}
+
+int fs_setup_plan(uint32_t n, uint32_t chunks, uint64_t* words, uint64_t wcap, uint64_t* nwords,
+                  uint32_t* layers4, uint32_t lcap, uint32_t* nlayers, uint64_t* deficit) {
+    fs::SetupPlan p = fs::build_plan(n, chunks ? chunks : 1);
+    if (nwords) *nwords = p.words.size();
+    if (nlayers) *nlayers = (uint32_t)p.layers.size();
+    if (deficit) *deficit = p.deficit;
+    if (p.words.size() > wcap || p.layers.size() > lcap) return (words || layers4) ? FS_E_OVERFLOW : FS_OK;
+    if (words) std::copy(p.words.begin(), p.words.end(), words);
+    if (layers4)
+        for (size_t i = 0; i < p.layers.size(); ++i) {
+            layers4[4 * i] = p.layers[i].begin;
+            layers4[4 * i + 1] = p.layers[i].end;
+            layers4[4 * i + 2] = p.layers[i].dbl;
+            layers4[4 * i + 3] = 0;
+        }
+    return FS_OK;
+}
+
+int fs_find_wheel_offset(uint64_t* start, int32_t* index) {
+    if (!start || !index) return FS_E_ARG;
+    // residues coprime to 30 in wheel order; the gap from res[i] to the next
+    // one is the i-th entry of the mod-30 gap table {4,2,4,2,4,6,2,6}
+    static const int res[8] = {7, 11, 13, 17, 19, 23, 29, 1};
+    uint64_t n = *start;
+    while (n % 2 == 0 || n % 3 == 0 || n % 5 == 0) ++n;
+    int r = (int)(n % 30);
+    for (int i = 0; i < 8; ++i)
+        if (res[i] == r) *index = i;
+    *start = n;
+    return FS_OK;
+}
+
+int fs_is_prime(uint64_t p) { return fs::is_prime_u64(p) ? 1 : 0; }
+
+int fs_verify_factor(uint64_t p, uint32_t n, int32_t c) { return fs::verify_factor(p, n, c) ? 1 : 0; }
+
+}  // extern "C"

@@ -1,0 +1,461 @@
+// fs_kernels.cu -- the GPU kernels of the FactSieve search path (sm_103a).
+//
+//   gen_kernel          candidate generation: odd numbers of [low, high) with
+//                       no prime factor <= 113 that pass the base-2 strong
+//                       PRP test (reference kernels/getsegprimes.cl:170-239)
+//   sieve_kernel<S,F>   per candidate p: starting residue nstart!*R mod p from
+//                       the bit-layered power table (setup.cl:49-103), the
+//                       residue walk r <- r*(n+1) with the +-1 hit test for n
+//                       in [nstart, nend) (iterate.cl:54-80), and on the last
+//                       n-chunk the checksum s6 + s7 and the nmax round trip
+//                       (check.cl:50-109).  S selects where the starting
+//                       residue comes from, F whether this chunk finishes.
+//   setup_partial_kernel  one chunk of the power table for a tile of
+//                       candidates, into a per-chunk partial product (used
+//                       when there are too few candidates to fill the GPU)
+//   table_check_kernel  one-shot check of the setup plan against the direct
+//                       product 2*3*...*n mod the first candidate
+//                       (verifyslow/verifypow/verifyreduce/verifyresult.cl)
+//   imad_bench_kernel   dependency-free integer streams that measure the
+//                       IMAD / ALU pipe rates used as the roofline
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fs_arith.cuh"
+#include "fs_kernels.cuh"
+#include "fs_launch.h"
+
+namespace fs {
+
+// ============================================================ generator ====
+
+// Odd primes whose multiples the generator removes before the PRP test: the
+// mod-30 wheel (3, 5) and the reference's mask primes 7..113.
+static __device__ constexpr u32 kSmallQ[29] = {3,  5,  7,  11, 13, 17, 19, 23, 29,  31,  37,  41,  43,  47, 53,
+                                    59, 61, 67, 71, 73, 79, 83, 89, 97, 101, 103, 107, 109, 113};
+
+// Bits at 0, q, 2q, ... below 32: the divisibility pattern of 32 consecutive
+// odd numbers by q, anchored at a multiple of q.
+__host__ __device__ constexpr u32 pattern_of(u32 q) {
+    u32 m = 0;
+    for (u32 i = 0; i < 32; i += q) m |= 1u << i;
+    return m;
+}
+
+constexpr int kGenWarps = 8;
+constexpr int kGenQueue = 32 * 32;   // one slot per odd number of the warp's 32 words (at most 18 per word survive)
+
+// One "word" = 32 consecutive odd numbers o0 + 64 w + 2 i, i in [0, 32).
+__global__ void __launch_bounds__(kGenWarps * 32) gen_kernel(GenArgs a) {
+    __shared__ u32 queue[kGenWarps][kGenQueue];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const u64 stride = (u64)gridDim.x * blockDim.x;
+    for (u64 wb = (u64)blockIdx.x * blockDim.x; wb < a.nwords; wb += stride) {
+        const u64 w = wb + threadIdx.x;
+        const u32 w32 = (u32)w;          // the host keeps nwords below 2^32
+        u32 sv = 0;
+        if (w < a.nwords) {
+            u32 comp = 0;
+#pragma unroll
+            for (int j = 0; j < 29; ++j) {
+                const u32 q = kSmallQ[j];
+                // residue of the word's first number o0 + 64 w
+                u32 r = (a.r0[j] + 64u * (w32 % q)) % q;
+                // first i with q | r + 2i: i0 = (q - r) * (q+1)/2 mod q
+                u32 i0 = ((q - r) * ((q + 1) >> 1)) % q;
+                comp |= i0 < 32 ? (pattern_of(q) << i0) : 0u;
+            }
+            sv = ~comp;
+            const u64 base = a.o0 + 64 * w;
+            const u64 room = a.high - base;              // > 0 since base < high
+            const u64 nvalid = (room + 1) >> 1;         // odd numbers below high
+            if (nvalid < 32) sv &= (1u << nvalid) - 1u;
+        }
+        // warp-wide exclusive scan of survivor counts
+        const u32 cnt = __popc(sv);
+        u32 incl = cnt;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            u32 v = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= d) incl += v;
+        }
+        const u32 total = __shfl_sync(0xffffffffu, incl, 31);
+        u32 off = incl - cnt;
+        while (sv) {
+            int i = __ffs(sv) - 1;
+            sv &= sv - 1;
+            queue[warp][off++] = w32 * 32u + (u32)i;   // odd index relative to o0
+        }
+        __syncwarp();
+        for (u32 jb = 0; jb < total; jb += 32) {
+            const u32 j = jb + lane;
+            bool pass = false;
+            u64 n = 0;
+            if (j < total) {
+                n = a.o0 + 2 * (u64)queue[warp][j];
+                pass = sprp2(n);
+            }
+            const u32 bal = __ballot_sync(0xffffffffu, pass);
+            if (bal) {
+                u32 base = 0;
+                if (lane == 0) base = atomicAdd(&a.ctr->ncand, (u32)__popc(bal));
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (pass) {
+                    u32 slot = base + __popc(bal & ((1u << lane) - 1u));
+                    if (slot < a.cap) a.cand[slot] = n;
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// ================================================================ sieve ====
+
+constexpr int kSieveThreads = 256;
+constexpr int kHitStage = 128;
+
+struct HitStage {
+    Factor buf[kHitStage];
+    u32 n;
+};
+
+// Record a hit: lanes that hit together take consecutive slots of the block's
+// shared-memory stage with one shared atomic (warp-ballot compaction); a full
+// stage spills straight to the global list.
+__device__ __noinline__ void record_hit(HitStage& st, u64 p, int nc, Factor* hits, u32 hitcap,
+                                        Counters* ctr) {
+    const u32 mask = __activemask();
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    const u32 rank = __popc(mask & ((1u << lane) - 1u));
+    u32 base = 0;
+    if (lane == leader) base = atomicAdd(&st.n, (u32)__popc(mask));
+    base = __shfl_sync(mask, base, leader);
+    const u32 slot = base + rank;
+    if (slot < kHitStage) {
+        st.buf[slot].p = p;
+        st.buf[slot].nc = nc;
+        st.buf[slot].pad = 0;
+    } else {
+        u32 g = atomicAdd(&ctr->nhits, 1u);
+        if (g < hitcap) {
+            hits[g].p = p;
+            hits[g].nc = nc;
+            hits[g].pad = 0;
+        } else {
+            atomicOr(&ctr->flags, FLAG_HIT_OVERFLOW);
+        }
+    }
+}
+
+// Product of one plan chunk's layers for candidate c, with its R^-deficit.
+__device__ __forceinline__ u64 plan_product(const Prime& c, const u64* __restrict__ words,
+                                            const Layer* __restrict__ layers, u32 lb, u32 le) {
+    const u64 p = c.p, pinv = c.pinv;
+    u64 x = c.one;
+    for (u32 l = lb; l < le; ++l) {
+        const Layer L = layers[l];
+        if (l != lb) x = mont_mul(x, x, p, pinv);
+        if (L.dbl) x = mod_add(x, x, p);
+        u32 i = L.begin;
+        if ((i & 1) && i < L.end) x = mont_mul(x, __ldg(words + i++), p, pinv);
+        for (; i + 2 <= L.end; i += 2) {
+            const ulonglong2 w2 = __ldg(reinterpret_cast<const ulonglong2*>(words + i));
+            x = mont_mul(x, w2.x, p, pinv);
+            x = mont_mul(x, w2.y, p, pinv);
+        }
+        if (i < L.end) x = mont_mul(x, __ldg(words + i), p, pinv);
+    }
+    return x;
+}
+
+// Walk n over [nstart, nend): test r = n!*R against +-R, then r <- r*(n+1).
+__device__ __forceinline__ u64 walk(u64 r, const Prime& c, u32 nstart, u32 nend, HitStage& st,
+                                    Factor* hits, u32 hitcap, Counters* ctr) {
+    const u64 p = c.p, one = c.one, nmo = p - one;
+    const u32 one_lo = (u32)one, nmo_lo = (u32)nmo;
+    if (nstart >= nend) return r;
+    const bool t64 = p > (1ull << 33) && p <= (~0ull) / (u64)nend;
+    if (t64) {
+        const Barrett br = make_barrett(p);
+        u32 n = nstart;
+        for (; n + 4 <= nend; n += 4) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const u32 lo = (u32)r;
+                if (lo == one_lo || lo == nmo_lo) {
+                    if (r == one || r == nmo)
+                        record_hit(st, p, r == one ? -(int)(n + j) : (int)(n + j), hits, hitcap, ctr);
+                }
+                r = mul_small_t64(r, n + j + 1, p, br);
+            }
+        }
+        for (; n < nend; ++n) {
+            if (r == one || r == nmo) record_hit(st, p, r == one ? -(int)n : (int)n, hits, hitcap, ctr);
+            r = mul_small_t64(r, n + 1, p, br);
+        }
+    } else {
+        // generic: multiply by the Montgomery image of n+1, advanced by R
+        u64 k = to_mont((u64)nstart + 1, c);
+        for (u32 n = nstart; n < nend; ++n) {
+            if (r == one || r == nmo) record_hit(st, p, r == one ? -(int)n : (int)n, hits, hitcap, ctr);
+            r = mont_mul(r, k, p, c.pinv);
+            k = mod_add(k, one, p);
+        }
+    }
+    return r;
+}
+
+template <int SETUP, bool FINAL>
+__global__ void __launch_bounds__(kSieveThreads) sieve_kernel(SieveArgs a) {
+    __shared__ HitStage st;
+    __shared__ u64 wsum[kSieveThreads / 32];
+    __shared__ u32 wbad[kSieveThreads / 32];
+    if (threadIdx.x == 0) st.n = 0;
+    __syncthreads();
+    const u32 ncand = *a.ncand;
+    const u32 n = ncand < a.cap ? ncand : a.cap;
+    u64 sum = 0;
+    u32 bad = 0;
+    const u32 stride = gridDim.x * blockDim.x;
+    for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const Prime c = make_prime(a.cand[i]);
+        u64 r;
+        if (SETUP == SETUP_PLAN) {
+            r = plan_product(c, a.plan.words, a.plan.layers, a.plan.layer_begin, a.plan.layer_end);
+            r = mont_mul(r, mont_pow(c.r2, a.plan.deficit, c), c.p, c.pinv);
+        } else if (SETUP == SETUP_PARTIALS) {
+            r = a.partials[i];
+            for (u32 k = 1; k < a.nchunks; ++k)
+                r = mont_mul(r, a.partials[(u64)k * a.cap + i], c.p, c.pinv);
+            r = mont_mul(r, mont_pow(c.r2, a.plan.deficit, c), c.p, c.pinv);
+        } else {
+            r = a.residue[i];
+        }
+        r = walk(r, c, a.nstart, a.nend, st, a.hits, a.hitcap, a.ctr);
+        if (FINAL) {
+            // s7 = nmax*R mod p, the reference's final Montgomery image of n
+            const u64 s7 = to_mont(a.nmax, c);
+            u32 back = (u32)mont_mul(s7, 1, c.p, c.pinv);
+            if (c.p <= a.nmax && a.nmax % c.p == back) back = a.nmax;
+            bad += back != a.nmax;
+            sum += r + s7;
+            if (a.store_final) a.residue[i] = r;
+        } else {
+            a.residue[i] = r;
+        }
+    }
+    if (FINAL) {
+        // warp then block reduction of the checksum, one atomic per block
+#pragma unroll
+        for (int d = 16; d; d >>= 1) {
+            sum += __shfl_xor_sync(0xffffffffu, sum, d);
+            bad += __shfl_xor_sync(0xffffffffu, bad, d);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            wsum[threadIdx.x >> 5] = sum;
+            wbad[threadIdx.x >> 5] = bad;
+        }
+    }
+    __syncthreads();
+    if (FINAL && threadIdx.x == 0) {
+        u64 s = 0;
+        u32 b = 0;
+        for (int w = 0; w < kSieveThreads / 32; ++w) {
+            s += wsum[w];
+            b += wbad[w];
+        }
+        if (s) atomicAdd(&a.ctr->raw_sum, s);
+        if (b) atomicOr(&a.ctr->flags, FLAG_VALIDATION);
+        if (blockIdx.x == 0 && a.count_candidates) {
+            atomicAdd(&a.ctr->primecount, (u64)ncand);
+            atomicMax(&a.ctr->maxcand, ncand);
+            if (ncand > a.cap) atomicOr(&a.ctr->flags, FLAG_CAND_OVERFLOW);
+        }
+    }
+    // flush the staged hits
+    const u32 nh = st.n < kHitStage ? st.n : kHitStage;
+    if (nh) {
+        __shared__ u32 gbase;
+        if (threadIdx.x == 0) gbase = atomicAdd(&a.ctr->nhits, nh);
+        __syncthreads();
+        for (u32 j = threadIdx.x; j < nh; j += blockDim.x) {
+            const u32 g = gbase + j;
+            if (g < a.hitcap)
+                a.hits[g] = st.buf[j];
+            else
+                atomicOr(&a.ctr->flags, FLAG_HIT_OVERFLOW);
+        }
+    }
+}
+
+// One chunk of the plan for candidates [0, n): partials[chunk * cap + i].
+__global__ void __launch_bounds__(kSieveThreads) setup_partial_kernel(SieveArgs a) {
+    const u32 ncand = *a.ncand;
+    const u32 n = ncand < a.cap ? ncand : a.cap;
+    const u32 chunk = blockIdx.y;
+    const PlanChunkDev pc = a.chunks[chunk];
+    const u32 stride = gridDim.x * blockDim.x;
+    for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const Prime c = make_prime(a.cand[i]);
+        a.partials[(u64)chunk * a.cap + i] =
+            plan_product(c, a.plan.words, a.plan.layers, pc.layer_begin, pc.layer_end);
+    }
+}
+
+// ========================================================== table check ====
+
+// Direct product 2*3*...*n0 mod the first candidate, reduced over the grid
+// (the last block to finish combines), against the plan's product.
+__global__ void __launch_bounds__(256) table_check_kernel(TableCheckArgs a) {
+    __shared__ u64 part[256];
+    __shared__ bool last;
+    if (*a.ncand == 0) return;
+    const Prime c = make_prime(a.cand[0]);
+    u64 acc = c.one;   // deficit grows by one per factor k
+    const u32 stride = gridDim.x * blockDim.x;
+    for (u64 k = 2 + blockIdx.x * blockDim.x + threadIdx.x; k <= a.n0; k += stride)
+        acc = mont_mul(acc, k, c.p, c.pinv);
+    part[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = 128; s; s >>= 1) {
+        if (threadIdx.x < s) part[threadIdx.x] = mont_mul(part[threadIdx.x], part[threadIdx.x + s], c.p, c.pinv);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        a.scratch[blockIdx.x] = part[0];
+        __threadfence();
+        u32 done = atomicAdd(a.done, 1u);
+        last = (done == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return;
+    __threadfence();
+    u64 direct = c.one;
+    for (u32 b = 0; b < gridDim.x; ++b) direct = mont_mul(direct, ((volatile u64*)a.scratch)[b], c.p, c.pinv);
+    const u64 nk = a.n0 >= 2 ? (u64)a.n0 - 1 : 0;
+    direct = mont_mul(direct, mont_pow(c.r2, nk, c), c.p, c.pinv);
+    u64 table = c.one;
+    for (u32 k = 0; k < a.nchunks; ++k) {
+        const u64 part_k = plan_product(c, a.words, a.layers, a.chunks[k].layer_begin, a.chunks[k].layer_end);
+        table = mont_mul(table, part_k, c.p, c.pinv);
+    }
+    // the chunks' deficits add; table now carries R^(1 - D) with one extra R^-1
+    // per combining product beyond the first -- combining started from one:
+    // mont_mul(one, x) = x, so no extra deficit.
+    table = mont_mul(table, mont_pow(c.r2, a.deficit, c), c.p, c.pinv);
+    a.result[0] = direct;
+    a.result[1] = table;
+    *a.done = 0;
+    if (direct != table) atomicOr(&a.ctr->flags, FLAG_TABLE);
+}
+
+// ============================================================ IMAD rate ====
+
+// kind 0: IMAD (mad.lo.u32), 1: IMAD.WIDE (mad.wide.u32), 2: IMAD.HI
+// (mul.hi.u32), 3: integer ALU (lop3/xor-add).  Eight independent chains per
+// thread; the result is stored so the work cannot be dropped.
+__global__ void __launch_bounds__(256) imad_bench_kernel(u32 iters, u32 kind, u32 seed, u32* sink) {
+    u32 a0 = seed ^ threadIdx.x, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3;
+    u32 a4 = a0 + 4, a5 = a0 + 5, a6 = a0 + 6, a7 = a0 + 7;
+    const u32 b = 0x9E3779B1u ^ seed, cc = 0x7F4A7C15u;
+    if (kind == 0) {
+        for (u32 it = 0; it < iters; ++it) {
+            asm volatile(
+                "mad.lo.u32 %0, %0, %8, %9;\n\tmad.lo.u32 %1, %1, %8, %9;\n\t"
+                "mad.lo.u32 %2, %2, %8, %9;\n\tmad.lo.u32 %3, %3, %8, %9;\n\t"
+                "mad.lo.u32 %4, %4, %8, %9;\n\tmad.lo.u32 %5, %5, %8, %9;\n\t"
+                "mad.lo.u32 %6, %6, %8, %9;\n\tmad.lo.u32 %7, %7, %8, %9;"
+                : "+r"(a0), "+r"(a1), "+r"(a2), "+r"(a3), "+r"(a4), "+r"(a5), "+r"(a6), "+r"(a7)
+                : "r"(b), "r"(cc));
+        }
+    } else if (kind == 1) {
+        u64 w0 = a0, w1 = a1, w2 = a2, w3 = a3, w4 = a4, w5 = a5, w6 = a6, w7 = a7;
+        for (u32 it = 0; it < iters; ++it) {
+            asm volatile(
+                "{.reg .u32 l0,l1,l2,l3,l4,l5,l6,l7;\n\t"
+                "cvt.u32.u64 l0, %0;\n\tcvt.u32.u64 l1, %1;\n\tcvt.u32.u64 l2, %2;\n\tcvt.u32.u64 l3, %3;\n\t"
+                "cvt.u32.u64 l4, %4;\n\tcvt.u32.u64 l5, %5;\n\tcvt.u32.u64 l6, %6;\n\tcvt.u32.u64 l7, %7;\n\t"
+                "mad.wide.u32 %0, l0, %8, %0;\n\tmad.wide.u32 %1, l1, %8, %1;\n\t"
+                "mad.wide.u32 %2, l2, %8, %2;\n\tmad.wide.u32 %3, l3, %8, %3;\n\t"
+                "mad.wide.u32 %4, l4, %8, %4;\n\tmad.wide.u32 %5, l5, %8, %5;\n\t"
+                "mad.wide.u32 %6, l6, %8, %6;\n\tmad.wide.u32 %7, l7, %8, %7;}"
+                : "+l"(w0), "+l"(w1), "+l"(w2), "+l"(w3), "+l"(w4), "+l"(w5), "+l"(w6), "+l"(w7)
+                : "r"(b));
+        }
+        a0 = (u32)(w0 ^ (w0 >> 32)) ^ (u32)(w1 ^ (w1 >> 32)) ^ (u32)(w2 ^ (w2 >> 32)) ^ (u32)(w3 ^ (w3 >> 32));
+        a1 = (u32)(w4 ^ (w4 >> 32)) ^ (u32)(w5 ^ (w5 >> 32)) ^ (u32)(w6 ^ (w6 >> 32)) ^ (u32)(w7 ^ (w7 >> 32));
+        a2 = a3 = a4 = a5 = a6 = a7 = 0;
+    } else if (kind == 2) {
+        for (u32 it = 0; it < iters; ++it) {
+            asm volatile(
+                "mul.hi.u32 %0, %0, %8;\n\tmul.hi.u32 %1, %1, %8;\n\t"
+                "mul.hi.u32 %2, %2, %8;\n\tmul.hi.u32 %3, %3, %8;\n\t"
+                "mul.hi.u32 %4, %4, %8;\n\tmul.hi.u32 %5, %5, %8;\n\t"
+                "mul.hi.u32 %6, %6, %8;\n\tmul.hi.u32 %7, %7, %8;"
+                : "+r"(a0), "+r"(a1), "+r"(a2), "+r"(a3), "+r"(a4), "+r"(a5), "+r"(a6), "+r"(a7)
+                : "r"(b | 0x80000000u));
+        }
+    } else {
+        for (u32 it = 0; it < iters; ++it) {
+            asm volatile(
+                "lop3.b32 %0, %0, %8, %9, 0x96;\n\tlop3.b32 %1, %1, %8, %9, 0x96;\n\t"
+                "lop3.b32 %2, %2, %8, %9, 0x96;\n\tlop3.b32 %3, %3, %8, %9, 0x96;\n\t"
+                "lop3.b32 %4, %4, %8, %9, 0x96;\n\tlop3.b32 %5, %5, %8, %9, 0x96;\n\t"
+                "lop3.b32 %6, %6, %8, %9, 0x96;\n\tlop3.b32 %7, %7, %8, %9, 0x96;"
+                : "+r"(a0), "+r"(a1), "+r"(a2), "+r"(a3), "+r"(a4), "+r"(a5), "+r"(a6), "+r"(a7)
+                : "r"(b), "r"(cc));
+        }
+    }
+    const u32 x = a0 ^ a1 ^ a2 ^ a3 ^ a4 ^ a5 ^ a6 ^ a7;
+    if (x == seed) sink[blockIdx.x] = x;   // practically never true, but not provable
+}
+
+// ============================================================== launches ===
+
+cudaError_t launch_gen(const GenArgs& a, int grid, cudaStream_t s) {
+    gen_kernel<<<grid, kGenWarps * 32, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sieve(const SieveArgs& a, int setup, bool final_chunk, int grid, cudaStream_t s) {
+    const int t = kSieveThreads;
+    if (setup == SETUP_PLAN) {
+        if (final_chunk) sieve_kernel<SETUP_PLAN, true><<<grid, t, 0, s>>>(a);
+        else sieve_kernel<SETUP_PLAN, false><<<grid, t, 0, s>>>(a);
+    } else if (setup == SETUP_PARTIALS) {
+        if (final_chunk) sieve_kernel<SETUP_PARTIALS, true><<<grid, t, 0, s>>>(a);
+        else sieve_kernel<SETUP_PARTIALS, false><<<grid, t, 0, s>>>(a);
+    } else {
+        if (final_chunk) sieve_kernel<SETUP_LOAD, true><<<grid, t, 0, s>>>(a);
+        else sieve_kernel<SETUP_LOAD, false><<<grid, t, 0, s>>>(a);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_setup_partial(const SieveArgs& a, int grid_x, int nchunks, cudaStream_t s) {
+    dim3 g(grid_x, nchunks);
+    setup_partial_kernel<<<g, kSieveThreads, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_table_check(const TableCheckArgs& a, int grid, cudaStream_t s) {
+    table_check_kernel<<<grid, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_imad_bench(u32 iters, u32 kind, u32 seed, u32* sink, int grid, cudaStream_t s) {
+    imad_bench_kernel<<<grid, 256, 0, s>>>(iters, kind, seed, sink);
+    return cudaGetLastError();
+}
+
+int sieve_threads() { return kSieveThreads; }
+int gen_threads() { return kGenWarps * 32; }
+
+cudaError_t sieve_occupancy(int* blocks_per_sm) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, sieve_kernel<SETUP_PLAN, true>,
+                                                         kSieveThreads, 0);
+}
+
+}  // namespace fs

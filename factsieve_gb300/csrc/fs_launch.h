@@ -1,0 +1,70 @@
+// fs_launch.h -- kernel argument blocks and launch wrappers (host <-> device).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fs_kernels.cuh"
+
+namespace fs {
+
+enum { SETUP_LOAD = 0, SETUP_PLAN = 1, SETUP_PARTIALS = 2 };
+
+// Candidate generator over the odd numbers o0 + 2 j < high.
+struct GenArgs {
+    u64 o0;          // first odd number >= low
+    u64 high;        // exclusive
+    u64 nwords;      // ceil((high - o0) / 64): words of 32 odd numbers
+    u32 r0[29];      // o0 mod q for the 29 sieving primes 3..113
+    u32 cap;         // capacity of cand[]
+    u64* cand;       // out: candidates (unordered)
+    Counters* ctr;   // ctr->ncand counts every candidate found, even past cap
+};
+
+struct PlanChunkDev {
+    u32 layer_begin, layer_end;
+    u64 deficit;
+};
+
+struct SieveArgs {
+    const u64* cand;      // candidates
+    const u32* ncand;     // device count (read by the kernel)
+    u32 cap;              // capacity of cand[] / residue[]
+    u64* residue;         // starting residues (SETUP_LOAD), updated residues (non-final)
+    u64* partials;        // SETUP_PARTIALS: nchunks x cap partial products
+    u32 nchunks;
+    const PlanChunkDev* chunks;
+    PlanDev plan;         // words/layers; layer range and total deficit for SETUP_PLAN
+    u32 nstart, nend;     // walk n over [nstart, nend)
+    u32 nmax;             // final n (s7 = nmax * R) on the final chunk
+    u32 count_candidates; // final chunk adds ncand to the candidate total
+    u32 store_final;      // final chunk also writes the end residues to residue[]
+    Factor* hits;
+    u32 hitcap;
+    Counters* ctr;
+};
+
+struct TableCheckArgs {
+    const u64* cand;
+    const u32* ncand;
+    u32 n0;
+    const u64* words;
+    const Layer* layers;
+    const PlanChunkDev* chunks;
+    u32 nchunks;
+    u64 deficit;
+    u64* scratch;     // one u64 per block
+    u32* done;        // block completion counter (reset by the last block)
+    u64* result;      // [direct, table]
+    Counters* ctr;
+};
+
+cudaError_t launch_gen(const GenArgs& a, int grid, cudaStream_t s);
+cudaError_t launch_sieve(const SieveArgs& a, int setup, bool final_chunk, int grid, cudaStream_t s);
+cudaError_t launch_setup_partial(const SieveArgs& a, int grid_x, int nchunks, cudaStream_t s);
+cudaError_t launch_table_check(const TableCheckArgs& a, int grid, cudaStream_t s);
+cudaError_t launch_imad_bench(u32 iters, u32 kind, u32 seed, u32* sink, int grid, cudaStream_t s);
+cudaError_t sieve_occupancy(int* blocks_per_sm);
+int sieve_threads();
+int gen_threads();
+
+}  // namespace fs

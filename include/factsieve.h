@@ -1,0 +1,172 @@
+/*
+ * factsieve.h -- C ABI of the GB300 FactSieve sieve (libfactsieve.so).
+ *
+ * The library replaces the reference's device layer: the OpenCL shim
+ * (simpleCL.h:67-117) plus the kernels getsegprimes, setup, iterate, check,
+ * clearn, clearresult and verify* (kernels/*.cl), and carries the host
+ * pieces of the same path (power table, CPU factor verification).  Every
+ * function returns a status code (FS_OK or FS_E_*) and never exits the
+ * process; the reference printed and called exit() on any error
+ * (simpleCL.c:347, cl_sieve.cpp:451-476).
+ *
+ * Threading: one fs_ctx per host thread; calls on one context are not
+ * thread-safe.  Device buffers of a search belong to the context; host
+ * arrays belong to the caller.  Functions taking d_* pointers want device
+ * memory the caller owns (any allocator); they run asynchronously on the
+ * context's stream.
+ */
+#ifndef FACTSIEVE_H
+#define FACTSIEVE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FS_OK 0
+#define FS_E_ARG 1         /* bad argument (the reference's range checks, main.cpp:51-65, cl_sieve.cpp:561-589) */
+#define FS_E_CUDA 2        /* a CUDA call failed; fs_last_error() has the text */
+#define FS_E_OVERFLOW 3    /* candidate or factor buffer full (cl_sieve.cpp:451-455, 473-476) */
+#define FS_E_VALIDATION 4  /* nmax round trip failed (check.cl:67-78, cl_sieve.cpp:463-467) */
+#define FS_E_TABLE 5       /* power table disagrees with the direct product (verify*.cl, cl_sieve.cpp:903-907) */
+#define FS_E_NOMEM 6       /* device or host allocation failed */
+#define FS_E_VERIFY 7      /* a hit failed CPU verification (cl_sieve.cpp:502-506) */
+#define FS_E_STATE 8       /* call out of order (e.g. segment before begin) */
+#define FS_E_TIMEOUT 9     /* a bounded wait gave up */
+
+/* Factor record, layout of the reference's `factor` (cl_sieve.h:3-6):
+ * nc = -n for p | n! - 1, +n for p | n! + 1 (iterate.cl:69-73). */
+typedef struct {
+    uint64_t p;
+    int32_t nc;
+    int32_t pad;
+} fs_factor;
+
+/* Device-resident counters shared by the stage-level kernels; the role of
+ * the reference's g_primecount[6] and g_sum[] (clearn.cl, clearresult.cl,
+ * check.cl:88-109). */
+typedef struct {
+    uint64_t raw_sum;     /* sum of (s6 + s7) over checked candidates, mod 2^64 */
+    uint64_t primecount;  /* candidates counted by fs_check / segments */
+    uint32_t ncand;       /* candidates written by fs_getsegprimes (may exceed capacity) */
+    uint32_t nhits;       /* factor hits found by fs_iterate (may exceed capacity) */
+    uint32_t flags;       /* FS_FLAG_* */
+    uint32_t maxcand;     /* largest candidate count of one segment */
+} fs_counters;
+
+#define FS_FLAG_VALIDATION 1u
+#define FS_FLAG_CAND_OVERFLOW 2u
+#define FS_FLAG_HIT_OVERFLOW 4u
+#define FS_FLAG_TABLE 8u
+
+typedef struct fs_ctx fs_ctx;
+
+/* Launch tuning; zero fields mean "choose automatically". */
+typedef struct {
+    uint32_t sieve_blocks_per_sm;   /* resident 256-thread sieve blocks per SM */
+    uint32_t gen_blocks_per_sm;     /* candidate-generator blocks per SM */
+    uint32_t max_steps_per_launch;  /* split the n-range into launches of at most this many steps */
+    uint32_t setup_chunks;          /* split the power table across this many threads per prime (1 = never) */
+} fs_tuning;
+
+/* ---- library / device ---------------------------------------------------- */
+int fs_version(void);
+const char *fs_strerror(int code);
+const char *fs_last_error(fs_ctx *ctx);
+int fs_device_count(int *count);
+
+/* Create a context on CUDA device `device` (replaces main.cpp:223-275 and
+ * the program/buffer set-up of cl_sieve.cpp:928-958). */
+int fs_create(int device, fs_ctx **out);
+int fs_destroy(fs_ctx *ctx);
+/* Run on an existing cudaStream_t (NULL: the context's own stream). */
+int fs_set_stream(fs_ctx *ctx, void *stream);
+void *fs_get_stream(fs_ctx *ctx);
+int fs_set_tuning(fs_ctx *ctx, const fs_tuning *t);
+int fs_get_tuning(fs_ctx *ctx, fs_tuning *t);
+int fs_device_info(fs_ctx *ctx, int *sm_count, int *clock_khz, uint64_t *total_mem);
+int fs_synchronize(fs_ctx *ctx);
+
+/* ---- whole search (cl_sieve.cpp:918-1270) -------------------------------- */
+/* Start a search over p in [pmin, pmax), n in [nmin, nmax): builds and
+ * uploads the power table for nmin (cl_sieve.cpp:790-866), sizes the factor
+ * buffer (result_cap = 0: the reference's 1e6, or 3e7 when pmin < 2^32,
+ * cl_sieve.cpp:591-595), clears the counters (clearresult.cl). */
+int fs_search_begin(fs_ctx *ctx, uint64_t pmin, uint64_t pmax, uint32_t nmin, uint32_t nmax,
+                    uint32_t result_cap);
+/* Queue one p-segment [low, high): getsegprimes -> (first segment: power
+ * table check) -> setup -> iterate -> check, all on the stream, no host
+ * synchronisation (cl_sieve.cpp:1142-1230). */
+int fs_search_segment(fs_ctx *ctx, uint64_t low, uint64_t high);
+/* Wait for the queued work, copy out the hits found since the last collect
+ * (unsorted) and the sums, then clear them (getResults' device half,
+ * cl_sieve.cpp:439-483, and clearresult.cl).  Returns FS_E_OVERFLOW,
+ * FS_E_VALIDATION or FS_E_TABLE when the device flagged one. */
+int fs_search_collect(fs_ctx *ctx, fs_factor *out, uint64_t cap, uint64_t *nfactors,
+                      uint64_t *raw_sum, uint64_t *primecount, uint32_t *flags);
+/* Convenience: queue segments of width seg_width (0: automatic) over
+ * [low, high). */
+int fs_search_range(fs_ctx *ctx, uint64_t low, uint64_t high, uint64_t seg_width);
+/* Capacity the context reserves for one segment of the given width. */
+uint64_t fs_candidate_capacity(uint64_t low, uint64_t high);
+
+/* ---- stage-level kernels on caller device buffers ------------------------ */
+/* getsegprimes (getsegprimes.cl:170-239): append the candidates of
+ * [low, high) to d_cand at slot d_ctr->ncand (the reference's
+ * g_primecount[0]).  Only the first `cap` slots are written. */
+int fs_getsegprimes(fs_ctx *ctx, uint64_t low, uint64_t high, uint64_t *d_cand, uint32_t cap,
+                    fs_counters *d_ctr);
+/* setup (setup.cl:49-103): d_residue[i] = nstart! * 2^64 mod d_cand[i] for
+ * i < min(d_ctr->ncand, cap). */
+int fs_setup(fs_ctx *ctx, const uint64_t *d_cand, uint32_t cap, fs_counters *d_ctr, uint32_t nstart,
+             uint64_t *d_residue);
+/* iterate (iterate.cl:54-80): advance residues from nstart! to nend!,
+ * appending hits to d_hits at d_ctr->nhits. */
+int fs_iterate(fs_ctx *ctx, const uint64_t *d_cand, uint32_t cap, fs_counters *d_ctr,
+               uint64_t *d_residue, uint32_t nstart, uint32_t nend, fs_factor *d_hits,
+               uint32_t hitcap);
+/* check (check.cl:50-109): add sum(s6 + s7) with s7 = nmax * 2^64 mod p to
+ * d_ctr->raw_sum, flag failed nmax round trips, add the candidate count to
+ * d_ctr->primecount. */
+int fs_check(fs_ctx *ctx, const uint64_t *d_cand, uint32_t cap, fs_counters *d_ctr,
+             const uint64_t *d_residue, uint32_t nmax);
+/* Power-table self-check (verifyslow/verifypow/verifyreduce/verifyresult.cl):
+ * compare nmin! from the table with the direct product modulo d_cand[0];
+ * sets FS_FLAG_TABLE in d_ctr->flags on mismatch.  out2 (host, may be NULL)
+ * receives {direct, table}. */
+int fs_table_check(fs_ctx *ctx, const uint64_t *d_cand, fs_counters *d_ctr, uint32_t nmin,
+                   uint64_t *out2);
+
+/* ---- measurement ---------------------------------------------------------- */
+/* Dependency-free integer stream on every SM: kind 0 IMAD, 1 IMAD.WIDE,
+ * 2 IMAD.HI, 3 LOP3.  Reports warp-lane operations per second. */
+int fs_bench_int_pipe(fs_ctx *ctx, uint32_t kind, uint32_t iters, double *ops_per_sec, double *ms);
+
+/* ---- host-side pieces (no GPU needed) -------------------------------------- */
+/* Reference-format power table for n! (cl_sieve.cpp:773-838). */
+int fs_power_table(uint32_t n, uint64_t *prime, uint32_t *exp, uint32_t *bit, uint32_t cap,
+                   uint32_t *len);
+/* The bit-layered setup plan the GPU uses for n!: words, layers as
+ * {begin, end, dbl, 0} quadruples, total R-deficit. */
+int fs_setup_plan(uint32_t n, uint32_t chunks, uint64_t *words, uint64_t wcap, uint64_t *nwords,
+                  uint32_t *layers4, uint32_t lcap, uint32_t *nlayers, uint64_t *deficit);
+/* First number >= *start coprime to 30 and its wheel index (cl_sieve.cpp:360-419). */
+int fs_find_wheel_offset(uint64_t *start, int32_t *index);
+/* 7-base deterministic Miller-Rabin (verifyprime.c:105-141). */
+int fs_is_prime(uint64_t p);
+/* Slow CPU check that p | n! + c (verifyprime.c:146-173). */
+int fs_verify_factor(uint64_t p, uint32_t n, int32_t c);
+/* getResults' CPU half (cl_sieve.cpp:484-550): sort hits by (p, |n|),
+ * verify each on `threads` CPU threads, drop hits whose p is not prime,
+ * compact the kept ones to the front.  *checksum_add = sum of (n + c) over
+ * kept hits (32-bit arithmetic as the reference).  Returns FS_E_VERIFY if
+ * any hit fails verification. */
+int fs_postprocess(fs_factor *f, uint64_t n, int threads, uint64_t *kept, uint64_t *checksum_add,
+                   uint64_t *discarded);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FACTSIEVE_H */

@@ -1,0 +1,194 @@
+"""GPU parity: the CUDA path through the C ABI against the oracle and the goldens.
+
+Every comparison is exact (integer work): candidate sets, residues, hit
+lists, checksums and prime counts must be bit-identical.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+# The reference's own self-test goldens (cl_sieve.cpp:1283-1364):
+# (pmin, pmax, nmin, nmax, factorcount, primecount, checksum)
+SELFTEST = {
+    1: (100_000_000, 101_000_000, 1_000_000, 2_000_000, 1071, 54211, 0x000004F4F744CA97),
+    2: (1_000_000_000_000, 1_000_010_000_000, 10_000, 2_000_000, 3, 361727, 0x05052A2D65F3D735),
+    3: (127, 100_000, 127, 1_000_000, 42770, 9566, 0x0000000065C074F0),
+    4: (2_000_000_000_000, 2_000_010_000_000, 2_000_000, 6_000_000, 3, 352866, 0x09C9742A908451EB),
+    5: (1_000_000_000_000, 1_000_001_000_000, 100_000_000, 110_000_000, 3, 36249, 0x0081056DC98DA092),
+}
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _dev_buffers(n_cand, n_hits=1 << 16):
+    torch = _torch()
+    cand = torch.zeros(max(n_cand, 1), dtype=torch.int64, device="cuda")
+    res = torch.zeros(max(n_cand, 1), dtype=torch.int64, device="cuda")
+    hits = torch.zeros(max(n_hits, 1) * 2, dtype=torch.int64, device="cuda")
+    ctr = torch.zeros(4, dtype=torch.int64, device="cuda")   # 32-byte fs_counters
+    return cand, res, hits, ctr
+
+
+def _u64(t):
+    return t.cpu().numpy().view(np.uint64)
+
+
+def _counters(ctr):
+    import factsieve_gb300 as fs
+    return np.frombuffer(ctr.cpu().numpy().tobytes(), dtype=fs.COUNTERS_DTYPE)[0]
+
+
+def _hits_array(hits, n):
+    import factsieve_gb300 as fs
+    raw = hits.cpu().numpy().tobytes()
+    return np.frombuffer(raw, dtype=fs.FACTOR_DTYPE, count=n).copy()
+
+
+def _sorted_hits(h):
+    return sorted(zip(h["p"].tolist(), h["nc"].tolist()))
+
+
+@pytest.mark.parametrize("idx", range(10))
+def test_candidates_match_oracle(ctx, idx):
+    with open(os.path.join(GOLD, "candidates_small.json")) as fh:
+        case = json.load(fh)[idx]
+    lo, hi, want = case["low"], case["high"], case["candidates"]
+    import factsieve_gb300 as fs
+    cap = fs.candidate_capacity(lo, hi)
+    cand, _, _, ctr = _dev_buffers(cap)
+    ctx.getsegprimes(lo, hi, cand.data_ptr(), cap, ctr.data_ptr())
+    ctx.synchronize()
+    c = _counters(ctr)
+    got = np.sort(_u64(cand)[: c["ncand"]])
+    assert c["ncand"] == len(want)
+    assert got.tolist() == sorted(want)
+
+
+def _golden(name):
+    path = os.path.join(GOLD, f"run_{name}.json")
+    if not os.path.exists(path):
+        pytest.skip(f"fixture {name} not generated")
+    with open(path) as fh:
+        return json.load(fh)
+
+
+@pytest.mark.parametrize("name", ["config1", "selftest3", "wilson_small", "top_of_u64", "near_2p32",
+                                  "near_2p62", "single_n", "nmin_eq_nmax"])
+def test_search_matches_golden(ctx, name):
+    g = _golden(name)
+    r = ctx.sieve(g["pmin"], g["pmax"], g["nmin"], g["nmax"], threads=8)
+    assert r.primecount == g["primecount"]
+    assert f"{r.raw_sum:016X}" == g["raw_sum"]
+    assert r.nhits == g["nhits"]
+    assert f"{r.checksum:016X}" == g["checksum"]
+    assert r.factorcount == g["factorcount"]
+    if "factors" in g:
+        assert r.lines() == g["factors"]
+
+
+@pytest.mark.parametrize("case", [1, 2, 4, 5])
+def test_reference_selftest(ctx, case):
+    pmin, pmax, nmin, nmax, fc, pc, cs = SELFTEST[case]
+    r = ctx.sieve(pmin, pmax, nmin, nmax, threads=16)
+    assert (r.factorcount, r.primecount, r.checksum) == (fc, pc, cs)
+
+
+def test_stage_api_matches_oracle(ctx, orc):
+    """getsegprimes -> setup -> iterate (two chunks) -> check against the oracle."""
+    lo, hi, nmin, nmax = 2_000_003, 2_060_000, 3000, 4500
+    want_c = orc.candidates(lo, hi)
+    import factsieve_gb300 as fs
+    cap = fs.candidate_capacity(lo, hi)
+    cand, res, hits, ctr = _dev_buffers(cap)
+    ctx.getsegprimes(lo, hi, cand.data_ptr(), cap, ctr.data_ptr())
+    ctx.setup(cand.data_ptr(), cap, ctr.data_ptr(), nmin, res.data_ptr())
+    ctx.iterate(cand.data_ptr(), cap, ctr.data_ptr(), res.data_ptr(), nmin, 3700, hits.data_ptr(), 1 << 16)
+    ctx.iterate(cand.data_ptr(), cap, ctr.data_ptr(), res.data_ptr(), 3700, nmax, hits.data_ptr(), 1 << 16)
+    ctx.check(cand.data_ptr(), cap, ctr.data_ptr(), res.data_ptr(), nmax)
+    ctx.synchronize()
+    c = _counters(ctr)
+    n = int(c["ncand"])
+    got_c = _u64(cand)[:n]
+    order = np.argsort(got_c)
+    assert got_c[order].tolist() == want_c.tolist()
+    want = orc.sieve_list(want_c, nmin, nmax, want_residues=True)
+    assert _u64(res)[:n][order].tolist() == want["s6"].tolist()
+    assert int(c["raw_sum"]) == want["raw_sum"]
+    assert int(c["primecount"]) == n
+    assert int(c["flags"]) == 0
+    assert _sorted_hits(_hits_array(hits, int(c["nhits"]))) == _sorted_hits(want["hits"])
+
+
+@pytest.mark.parametrize("nmin", [127, 1000, 54_321, 1_000_000])
+def test_setup_residue_matches_oracle(ctx, orc, nmin):
+    """nmin! * 2^64 mod p from the bit-layered table equals the reference table's."""
+    import factsieve_gb300 as fs
+    lo = max(nmin, 1_000_000_007)
+    hi = lo + 40_000
+    want_c = orc.candidates(lo, hi)
+    table = orc.power_table(nmin)
+    cap = fs.candidate_capacity(lo, hi)
+    cand, res, _, ctr = _dev_buffers(cap)
+    ctx.getsegprimes(lo, hi, cand.data_ptr(), cap, ctr.data_ptr())
+    ctx.setup(cand.data_ptr(), cap, ctr.data_ptr(), nmin, res.data_ptr())
+    ctx.synchronize()
+    n = int(_counters(ctr)["ncand"])
+    got_c = _u64(cand)[:n]
+    order = np.argsort(got_c)
+    got = _u64(res)[:n][order]
+    want = [orc.setup(int(p), table) for p in want_c[:200]]
+    assert got[:200].tolist() == want
+
+
+@pytest.mark.parametrize("nmin", [127, 5000, 1_000_000, 20_000_000])
+def test_table_check_agrees(ctx, nmin):
+    import factsieve_gb300 as fs
+    lo, hi = 1_000_000_000_039, 1_000_000_100_000
+    cap = fs.candidate_capacity(lo, hi)
+    cand, _, _, ctr = _dev_buffers(cap)
+    ctx.getsegprimes(lo, hi, cand.data_ptr(), cap, ctr.data_ptr())
+    direct, table = ctx.table_check(cand.data_ptr(), ctr.data_ptr(), nmin)
+    assert direct == table
+    assert int(_counters(ctr)["flags"]) == 0
+
+
+def test_split_launches_and_setup_chunks_agree(ctx):
+    """n-range split over launches and power table split over threads give the same bits."""
+    g = _golden("config1")
+    base = ctx.sieve(g["pmin"], g["pmax"], g["nmin"], g["nmax"])
+    try:
+        ctx.set_tuning(max_steps_per_launch=137, setup_chunks=5)
+        r = ctx.sieve(g["pmin"], g["pmax"], g["nmin"], g["nmax"])
+    finally:
+        ctx.set_tuning()
+    assert (r.raw_sum, r.primecount, r.checksum, r.lines()) == (base.raw_sum, base.primecount, base.checksum,
+                                                               base.lines())
+    assert f"{r.checksum:016X}" == g["checksum"]
+
+
+def test_small_segments_agree(ctx):
+    """Any segmentation of the p-range gives the same result (sums commute)."""
+    g = _golden("selftest3")
+    r = ctx.sieve(g["pmin"], g["pmax"], g["nmin"], g["nmax"], seg_width=7_777, threads=8)
+    assert f"{r.checksum:016X}" == g["checksum"]
+    assert r.primecount == g["primecount"]
+
+
+def test_hit_overflow_is_reported(ctx):
+    """A factor buffer that is too small yields FS_E_OVERFLOW, not silent loss."""
+    import factsieve_gb300 as fs
+    g = _golden("wilson_small")
+    ctx.begin(g["pmin"], g["pmax"], g["nmin"], g["nmax"], result_cap=10)
+    ctx.run_range(g["pmin"], g["pmax"])
+    hits, raw, pc, flags, rc = ctx.collect(10, raise_on_flags=False)
+    assert rc == fs.FS_E_OVERFLOW
+    assert flags & fs.FLAG_HIT_OVERFLOW
