@@ -49,9 +49,15 @@ class Factor(C.Structure):
     _fields_ = [("p", C.c_uint64), ("nc", C.c_int32), ("pad", C.c_int32)]
 
 
+class Stats(C.Structure):
+    _fields_ = [("launches", C.c_uint64), ("sieve_launches", C.c_uint64), ("gen_launches", C.c_uint64),
+                ("sieve_ms", C.c_double), ("gen_ms", C.c_double)]
+
+
 class Tuning(C.Structure):
     _fields_ = [("sieve_blocks_per_sm", C.c_uint32), ("gen_blocks_per_sm", C.c_uint32),
-                ("max_steps_per_launch", C.c_uint32), ("setup_chunks", C.c_uint32)]
+                ("max_steps_per_launch", C.c_uint32), ("setup_chunks", C.c_uint32),
+                ("sieve_variant", C.c_uint32)]
 
 
 _lock = threading.Lock()
@@ -85,6 +91,9 @@ def _declare(L):
         "fs_check": (C.c_int, [vp, vp, u32, vp, vp, u32]),
         "fs_table_check": (C.c_int, [vp, vp, vp, u32, P64]),
         "fs_bench_int_pipe": (C.c_int, [vp, u32, u32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+        "fs_set_timing": (C.c_int, [vp, C.c_int]),
+        "fs_get_stats": (C.c_int, [vp, C.POINTER(Stats)]),
+        "fs_reset_stats": (C.c_int, [vp]),
         "fs_power_table": (C.c_int, [u32, P64, P32, P32, u32, P32]),
         "fs_setup_plan": (C.c_int, [u32, u32, P64, u64, P64, P32, u32, P32, P64]),
         "fs_find_wheel_offset": (C.c_int, [P64, PI32]),
@@ -257,8 +266,8 @@ class Context:
         self._chk(lib().fs_set_stream(self._h, C.c_void_p(stream or 0)), "fs_set_stream")
 
     def set_tuning(self, sieve_blocks_per_sm=0, gen_blocks_per_sm=0, max_steps_per_launch=0,
-                   setup_chunks=0) -> None:
-        t = Tuning(sieve_blocks_per_sm, gen_blocks_per_sm, max_steps_per_launch, setup_chunks)
+                   setup_chunks=0, sieve_variant=0) -> None:
+        t = Tuning(sieve_blocks_per_sm, gen_blocks_per_sm, max_steps_per_launch, setup_chunks, sieve_variant)
         self._chk(lib().fs_set_tuning(self._h, C.byref(t)), "fs_set_tuning")
 
     def tuning(self) -> dict:
@@ -290,6 +299,17 @@ class Context:
         if rc and raise_on_flags:
             self._chk(rc, "fs_search_collect")
         return hits, rs.value, pc.value, fl.value, rc
+
+    def set_timing(self, enable: bool) -> None:
+        self._chk(lib().fs_set_timing(self._h, 1 if enable else 0), "fs_set_timing")
+
+    def stats(self) -> dict:
+        s = Stats()
+        self._chk(lib().fs_get_stats(self._h, C.byref(s)), "fs_get_stats")
+        return {k: getattr(s, k) for k, _ in Stats._fields_}
+
+    def reset_stats(self) -> None:
+        self._chk(lib().fs_reset_stats(self._h), "fs_reset_stats")
 
     def bench_int_pipe(self, kind: int, iters: int = 20000):
         ops, ms = C.c_double(0), C.c_double(0)

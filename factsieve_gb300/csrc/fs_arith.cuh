@@ -6,17 +6,17 @@
 // are used:
 //
 //   mont_mul(a, b)     a*b/R mod p for a < p, b < 2^64.  Setup and the PRP test.
-//   mul_small_t64(s,k) s*k mod p for a 32-bit k by a Barrett step, valid when
-//                      p > 2^33 and p*k < 2^64.  The iterate hot loop: the
-//                      multiplier k = n+1 is a plain integer, so multiplying a
-//                      Montgomery-form residue by it keeps the form and needs
-//                      no Montgomery image of n at all.
+//   lazy_step(r, k)    r*k mod p for a 32-bit k by a Barrett step on residues
+//                      kept in [0, 2p), valid when p > 2^33 and p*k <= 2^62.
+//                      The iterate hot loop: the multiplier k = n+1 is a plain
+//                      integer, so multiplying a Montgomery-form residue by it
+//                      keeps the form and needs no Montgomery image of n.
 //   mont_mul with kR   generic iterate step for every other (p, n) (the
 //                      reference's own step: multiply by the Montgomery image
 //                      of n+1, which advances by R each step).
 //
-// Every routine returns the canonical residue, so any mix of them yields the
-// same bits as the reference.
+// Residues leave every routine canonical (the lazy walk folds [0, 2p) back
+// into [0, p) at its end), so any mix of them yields the reference's bits.
 #pragma once
 #include <stdint.h>
 
@@ -120,47 +120,99 @@ __device__ __forceinline__ bool sprp2(u64 n) {
     return false;
 }
 
-// ------------------------------------------------- iterate: Barrett step --
-
-// Constants of the 32-bit-multiplier Barrett step for p in (2^33, 2^64/kmax).
-//   mu = floor(2^96 / p)  (< 2^63),  np = 2^64 - p.
-struct Barrett {
-    u64 mu, np;
+// ------------------------------------------- iterate: lazy Barrett step --
+//
+// For p in (2^33, 2^62 / kmax] the walk keeps r in [0, 2p) ("lazy") and
+// multiplies by the plain 32-bit k = n + 1 (p * k <= 2^62, so t = r k < 2^63):
+//
+//   z  = floor(t / 2^32)            (< 2^31)
+//   M  = floor(2^64 / p)            (< 2^31)
+//   qe = floor(z M / 2^32)          = floor(t/p) or one less, since
+//                                    t/p - z M / 2^32 < 2^32/p + z/2^32 < 1
+//   r' = t - qe p                   (in [0, 2p); computed mod 2^64 as t + qe (2^64 - p))
+//
+// Three 32-bit multiply groups (t, qe, qe p) and no correction step.  The
+// +-1 test looks at the low word of r against the four values one, one + p,
+// nmo, nmo + p that r can take when r = +-R mod p; a match is checked exactly
+// on the slow path.
+struct Lazy64 {
+    u64 p, one;               // one = R mod p
+    u32 np0, np1, M;          // 2^64 - p (two words), floor(2^64 / p)
+    u32 c0, c1, c2, c3;       // low words of one, one + p, p - one, 2p - one
 };
 
-// floor(2^96 / p) for odd p > 2^33: A = floor((2^64-1)/p) = floor(2^64/p),
-// rem = 2^64 - A p in [1, p), then 32 steps of binary long division of
-// rem * 2^32 by p supply the low 32 quotient bits.
-__device__ __forceinline__ Barrett make_barrett(u64 p) {
-    Barrett b;
-    u64 A = (~0ull) / p;
-    u64 rem = 0ull - A * p;                // 2^64 - A p (mod 2^64), in [1, p)
-    u32 lowq = 0;
-    for (int i = 0; i < 32; ++i) {
-        u64 top = rem >> 63;
-        rem <<= 1;
-        lowq <<= 1;
-        if (top || rem >= p) {
-            rem -= p;
-            lowq |= 1;
-        }
-    }
-    b.mu = (A << 32) | lowq;
-    b.np = 0ull - p;
-    return b;
+__device__ __forceinline__ Lazy64 make_lazy(const Prime& c) {
+    Lazy64 L;
+    L.p = c.p;
+    L.one = c.one;
+    const u64 np = 0ull - c.p;
+    L.np0 = (u32)np;
+    L.np1 = (u32)(np >> 32);
+    L.M = (u32)((~0ull) / c.p);
+    const u64 nmo = c.p - c.one;
+    L.c0 = (u32)c.one;
+    L.c1 = (u32)(c.one + c.p);
+    L.c2 = (u32)nmo;
+    L.c3 = (u32)(nmo + c.p);
+    return L;
 }
 
-// s*k mod p for s < p, k < 2^32, p > 2^33 and p*k < 2^64 (so t = s*k fits a
-// u64).  z = floor(t/2^32); qe = floor(z*mu/2^64) is floor(t/p) or one less
-// (the truncations cost < 2^32/p + 2^-32 < 1), so r = t - qe*p is in [0, 2p)
-// and one conditional subtraction makes it canonical.
-__device__ __forceinline__ u64 mul_small_t64(u64 s, u32 k, u64 p, const Barrett& br) {
-    u64 t = s * (u64)k;
-    u32 z = (u32)(t >> 32);
-    u64 hz = __umulhi(z, (u32)br.mu);                      // floor(z*mu_lo / 2^32)
-    u64 qe = ((u64)z * (br.mu >> 32) + hz) >> 32;          // floor(z*mu / 2^64)
-    u64 r = t + qe * br.np;                                // t - qe*p (mod 2^64)
-    return r >= p ? r - p : r;
+// p qualifies for the lazy step for every multiplier up to kmax.
+__device__ __forceinline__ bool lazy_ok(u64 p, u32 kmax) {
+    return p > (1ull << 33) && p <= ((1ull << 62) / (u64)(kmax ? kmax : 1));
+}
+
+// One lazy step r <- r*k (r in [0, 2p)), bit-identical to the PTX block below.
+__device__ __forceinline__ u64 lazy_step(u64 r, u32 k, const Lazy64& L) {
+    const u64 t = r * (u64)k;
+    const u32 qe = __umulhi((u32)(t >> 32), L.M);
+    return t + (u64)qe * (((u64)L.np1 << 32) | L.np0);
+}
+
+__device__ __forceinline__ u64 lazy_canon(u64 r, const Lazy64& L) { return r >= L.p ? r - L.p : r; }
+
+// Eight lazy steps on two independent residues (A in %0:%1, B in %2:%3)
+// with multipliers k1 .. k1+7.  Before each multiply the low words are
+// compared with the four hit values; the comparisons OR into one predicate
+// returned as 0/1 (a hit, or a 2^-30-rare low-word coincidence, somewhere in
+// the eight steps).
+#define FS_LZ_TEST(RL, C0, C1, C2, C3)                 \
+    "setp.eq.or.u32 P, " RL ", " C0 ", P;\n\t"         \
+    "setp.eq.or.u32 P, " RL ", " C1 ", P;\n\t"         \
+    "setp.eq.or.u32 P, " RL ", " C2 ", P;\n\t"         \
+    "setp.eq.or.u32 P, " RL ", " C3 ", P;\n\t"
+#define FS_LZ_MUL(RL, RH, NP0, NP1, MM, T, R, TL, TH, Q)          \
+    "mul.wide.u32 " T ", " RL ", kk;\n\t"                          \
+    "mov.b64 {" TL ", " TH "}, " T ";\n\t"                         \
+    "mad.lo.u32 " TH ", " RH ", kk, " TH ";\n\t"                   \
+    "mul.hi.u32 " Q ", " TH ", " MM ";\n\t"                        \
+    "mov.b64 " T ", {" TL ", " TH "};\n\t"                         \
+    "mad.wide.u32 " R ", " Q ", " NP0 ", " T ";\n\t"               \
+    "mov.b64 {" RL ", " RH "}, " R ";\n\t"                         \
+    "mad.lo.u32 " RH ", " Q ", " NP1 ", " RH ";\n\t"
+#define FS_LZ_STEP2(J)                                              \
+    "add.u32 kk, %5, " #J ";\n\t"                                   \
+    FS_LZ_TEST("%0", "%9", "%10", "%11", "%12")                     \
+    FS_LZ_TEST("%2", "%16", "%17", "%18", "%19")                    \
+    FS_LZ_MUL("%0", "%1", "%6", "%7", "%8", "TA", "RA", "aL", "aH", "qA") \
+    FS_LZ_MUL("%2", "%3", "%13", "%14", "%15", "TB", "RB", "bL", "bH", "qB")
+
+__device__ __forceinline__ u32 lazy_walk8x2(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const Lazy64& A,
+                                            const Lazy64& B) {
+    u32 flag;
+    asm("{\n\t"
+        ".reg .u32 kk, aL, aH, qA, bL, bH, qB;\n\t"
+        ".reg .u64 TA, RA, TB, RB;\n\t"
+        ".reg .pred P;\n\t"
+        "setp.ne.u32 P, %5, %5;\n\t"
+        FS_LZ_STEP2(0) FS_LZ_STEP2(1) FS_LZ_STEP2(2) FS_LZ_STEP2(3)
+        FS_LZ_STEP2(4) FS_LZ_STEP2(5) FS_LZ_STEP2(6) FS_LZ_STEP2(7)
+        "selp.u32 %4, 1, 0, P;\n\t"
+        "}"
+        : "+r"(al), "+r"(ah), "+r"(bl), "+r"(bh), "=r"(flag)
+        : "r"(k1), "r"(A.np0), "r"(A.np1), "r"(A.M), "r"(A.c0), "r"(A.c1), "r"(A.c2), "r"(A.c3),
+          "r"(B.np0), "r"(B.np1), "r"(B.M), "r"(B.c0), "r"(B.c1), "r"(B.c2), "r"(B.c3));
+    return flag;
 }
 
 }  // namespace fs

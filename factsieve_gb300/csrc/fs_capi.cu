@@ -46,7 +46,7 @@ struct fs_ctx {
     cudaStream_t own = nullptr, stream = nullptr;
     int sm_count = 0, clock_khz = 0;
     uint64_t total_mem = 0;
-    int sieve_occ = 1;
+    int sieve_occ[5] = {1, 1, 1, 1, 1};
     fs_tuning tuning{};
     std::string err;
     // search state
@@ -68,6 +68,11 @@ struct fs_ctx {
     int chk_grid = 0;
     u32* d_sink = nullptr;
     std::map<std::pair<uint32_t, uint32_t>, PlanGPU> plans;
+    // statistics
+    bool timing = false;
+    uint64_t launches = 0, sieve_launches = 0, gen_launches = 0;
+    double sieve_ms = 0, gen_ms = 0;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> sieve_ev, gen_ev, ev_pool;
 };
 
 #define CK(ctx, call)                                                          \
@@ -86,6 +91,42 @@ int bind(fs_ctx* c) {
     if (e != cudaSuccess) {
         c->err = std::string("cudaSetDevice: ") + cudaGetErrorString(e);
         return FS_E_CUDA;
+    }
+    return FS_OK;
+}
+
+// A pair of events around one launch when timing is on.
+int ev_begin(fs_ctx* c, std::pair<cudaEvent_t, cudaEvent_t>* ev) {
+    if (!c->timing) return FS_OK;
+    if (!c->ev_pool.empty()) {
+        *ev = c->ev_pool.back();
+        c->ev_pool.pop_back();
+    } else {
+        CK(c, cudaEventCreate(&ev->first));
+        CK(c, cudaEventCreate(&ev->second));
+    }
+    CK(c, cudaEventRecord(ev->first, c->stream));
+    return FS_OK;
+}
+
+int ev_end(fs_ctx* c, std::pair<cudaEvent_t, cudaEvent_t>& ev, std::vector<std::pair<cudaEvent_t, cudaEvent_t>>& list) {
+    if (!c->timing) return FS_OK;
+    CK(c, cudaEventRecord(ev.second, c->stream));
+    list.push_back(ev);
+    return FS_OK;
+}
+
+int ev_drain(fs_ctx* c) {
+    for (int k = 0; k < 2; ++k) {
+        auto& list = k ? c->gen_ev : c->sieve_ev;
+        for (auto& ev : list) {
+            CK(c, cudaEventSynchronize(ev.second));
+            float ms = 0;
+            CK(c, cudaEventElapsedTime(&ms, ev.first, ev.second));
+            (k ? c->gen_ms : c->sieve_ms) += ms;
+            c->ev_pool.push_back(ev);
+        }
+        list.clear();
     }
     return FS_OK;
 }
@@ -164,8 +205,13 @@ fs::SieveArgs base_args(PlanGPU* pl) {
     return a;
 }
 
+int variant(fs_ctx* c) {
+    const uint32_t v = c->tuning.sieve_variant;
+    return (v == 2 || v == 3 || v == 4) ? (int)v : 3;
+}
+
 int sieve_grid(fs_ctx* c) {
-    int bpsm = c->tuning.sieve_blocks_per_sm ? (int)c->tuning.sieve_blocks_per_sm : c->sieve_occ;
+    int bpsm = c->tuning.sieve_blocks_per_sm ? (int)c->tuning.sieve_blocks_per_sm : c->sieve_occ[variant(c)];
     return std::max(1, c->sm_count * bpsm);
 }
 
@@ -201,8 +247,13 @@ int run_gen(fs_ctx* c, uint64_t low, uint64_t high, u64* d_cand, uint32_t cap, f
     const int threads = fs::gen_threads();
     uint64_t blocks = (g.nwords + threads - 1) / threads;
     uint64_t maxb = (uint64_t)c->sm_count * (c->tuning.gen_blocks_per_sm ? c->tuning.gen_blocks_per_sm : 8);
+    std::pair<cudaEvent_t, cudaEvent_t> ev;
+    int rc = ev_begin(c, &ev);
+    if (rc) return rc;
     CK(c, fs::launch_gen(g, (int)std::max<uint64_t>(1, std::min(blocks, maxb)), c->stream));
-    return FS_OK;
+    ++c->launches;
+    ++c->gen_launches;
+    return ev_end(c, ev, c->gen_ev);
 }
 
 int run_table_check(fs_ctx* c, const u64* d_cand, fs::Counters* d_ctr, uint32_t n, PlanGPU* pl) {
@@ -229,6 +280,7 @@ int run_table_check(fs_ctx* c, const u64* d_cand, fs::Counters* d_ctr, uint32_t 
     t.ctr = d_ctr;
     CK(c, cudaMemsetAsync(c->d_chk_result, 0, 2 * sizeof(u64), c->stream));
     CK(c, fs::launch_table_check(t, c->chk_grid, c->stream));
+    ++c->launches;
     return FS_OK;
 }
 
@@ -263,7 +315,12 @@ int run_sieve(fs_ctx* c, const u64* d_cand, uint32_t cap, fs::Counters* d_ctr, u
         if ((rc = grow(c, &c->d_partials, &c->partials_cap, (uint64_t)cap * chunks + 1))) return rc;
         a.partials = c->d_partials;
         int gx = std::max(1, sieve_grid(c) / (int)chunks);
+        std::pair<cudaEvent_t, cudaEvent_t> ev;
+        if ((rc = ev_begin(c, &ev))) return rc;
         CK(c, fs::launch_setup_partial(a, gx, (int)chunks, c->stream));
+        if ((rc = ev_end(c, ev, c->sieve_ev))) return rc;
+        ++c->launches;
+        ++c->sieve_launches;
         setup_mode = fs::SETUP_PARTIALS;
     }
     uint32_t s = nstart;
@@ -276,7 +333,12 @@ int run_sieve(fs_ctx* c, const u64* d_cand, uint32_t cap, fs::Counters* d_ctr, u
         a.residue = split ? c->d_residue : nullptr;
         a.count_candidates = (fin && count) ? 1u : 0u;
         a.store_final = 0;
-        CK(c, fs::launch_sieve(a, first ? setup_mode : fs::SETUP_LOAD, fin, grid, c->stream));
+        std::pair<cudaEvent_t, cudaEvent_t> ev;
+        if ((rc = ev_begin(c, &ev))) return rc;
+        CK(c, fs::launch_sieve(a, first ? setup_mode : fs::SETUP_LOAD, fin, grid, c->stream, variant(c)));
+        if ((rc = ev_end(c, ev, c->sieve_ev))) return rc;
+        ++c->launches;
+        ++c->sieve_launches;
         first = false;
         s = e;
     } while (s < nend);
@@ -350,8 +412,10 @@ int fs_create(int device, fs_ctx** out) {
     cudaDeviceGetAttribute(&clk, cudaDevAttrClockRate, device);
     c->clock_khz = clk;
     c->total_mem = prop.totalGlobalMem;
-    int occ = 0;
-    if (fs::sieve_occupancy(&occ) == cudaSuccess && occ > 0) c->sieve_occ = occ;
+    for (int v = 2; v <= 4; ++v) {
+        int occ = 0;
+        if (fs::sieve_occupancy(&occ, v) == cudaSuccess && occ > 0) c->sieve_occ[v] = occ;
+    }
     if (cudaMalloc((void**)&c->d_ctr, sizeof(fs::Counters)) != cudaSuccess ||
         cudaMalloc((void**)&c->d_sink, 4096 * sizeof(u32)) != cudaSuccess) {
         cudaStreamDestroy(c->own);
@@ -377,8 +441,42 @@ int fs_destroy(fs_ctx* c) {
     cudaFree(c->d_chk_done);
     cudaFree(c->d_chk_result);
     cudaFree(c->d_sink);
+    for (auto* l : {&c->sieve_ev, &c->gen_ev, &c->ev_pool})
+        for (auto& ev : *l) {
+            cudaEventDestroy(ev.first);
+            cudaEventDestroy(ev.second);
+        }
     if (c->own) cudaStreamDestroy(c->own);
     delete c;
+    return FS_OK;
+}
+
+int fs_set_timing(fs_ctx* c, int enable) {
+    if (!c) return FS_E_ARG;
+    c->timing = enable != 0;
+    return FS_OK;
+}
+
+int fs_get_stats(fs_ctx* c, fs_stats* out) {
+    if (!c || !out) return FS_E_ARG;
+    int rc = bind(c);
+    if (rc) return rc;
+    if ((rc = ev_drain(c))) return rc;
+    out->launches = c->launches;
+    out->sieve_launches = c->sieve_launches;
+    out->gen_launches = c->gen_launches;
+    out->sieve_ms = c->sieve_ms;
+    out->gen_ms = c->gen_ms;
+    return FS_OK;
+}
+
+int fs_reset_stats(fs_ctx* c) {
+    if (!c) return FS_E_ARG;
+    int rc = bind(c);
+    if (rc) return rc;
+    if ((rc = ev_drain(c))) return rc;
+    c->launches = c->sieve_launches = c->gen_launches = 0;
+    c->sieve_ms = c->gen_ms = 0;
     return FS_OK;
 }
 
@@ -399,7 +497,8 @@ int fs_set_tuning(fs_ctx* c, const fs_tuning* t) {
 int fs_get_tuning(fs_ctx* c, fs_tuning* t) {
     if (!c || !t) return FS_E_ARG;
     *t = c->tuning;
-    if (!t->sieve_blocks_per_sm) t->sieve_blocks_per_sm = (uint32_t)c->sieve_occ;
+    if (!t->sieve_variant) t->sieve_variant = (uint32_t)variant(c);
+    if (!t->sieve_blocks_per_sm) t->sieve_blocks_per_sm = (uint32_t)c->sieve_occ[variant(c)];
     return FS_OK;
 }
 
@@ -447,6 +546,9 @@ int fs_search_begin(fs_ctx* c, uint64_t pmin, uint64_t pmax, uint32_t nmin, uint
     c->nmax = nmax;
     c->active = true;
     c->table_checked = false;
+    // a search builds and uploads its own power table (cl_sieve.cpp:1159)
+    CK(c, cudaStreamSynchronize(c->stream));
+    free_plans(c);
     uint32_t cap = result_cap ? result_cap : (pmin < 0xFFFFFFFFull ? 30000000u : 1000000u);
     uint64_t have = c->hit_cap;
     if ((rc = grow(c, &c->d_hits, &have, cap))) return rc;
@@ -553,7 +655,7 @@ int fs_setup(fs_ctx* c, const uint64_t* d_cand, uint32_t cap, fs_counters* d_ctr
         CK(c, fs::launch_setup_partial(a, std::max(1, sieve_grid(c) / (int)chunks), (int)chunks, c->stream));
         mode = fs::SETUP_PARTIALS;
     }
-    CK(c, fs::launch_sieve(a, mode, false, sieve_grid(c), c->stream));
+    CK(c, fs::launch_sieve(a, mode, false, sieve_grid(c), c->stream, variant(c)));
     return FS_OK;
 }
 
@@ -577,7 +679,7 @@ int fs_iterate(fs_ctx* c, const uint64_t* d_cand, uint32_t cap, fs_counters* d_c
         uint32_t e = (maxs && nend - s > maxs) ? s + maxs : nend;
         a.nstart = s;
         a.nend = e;
-        CK(c, fs::launch_sieve(a, fs::SETUP_LOAD, false, sieve_grid(c), c->stream));
+        CK(c, fs::launch_sieve(a, fs::SETUP_LOAD, false, sieve_grid(c), c->stream, variant(c)));
         s = e;
     } while (s < nend);
     return FS_OK;
@@ -598,7 +700,7 @@ int fs_check(fs_ctx* c, const uint64_t* d_cand, uint32_t cap, fs_counters* d_ctr
     a.nmax = nmax;
     a.count_candidates = 1;
     a.store_final = 0;
-    CK(c, fs::launch_sieve(a, fs::SETUP_LOAD, true, sieve_grid(c), c->stream));
+    CK(c, fs::launch_sieve(a, fs::SETUP_LOAD, true, sieve_grid(c), c->stream, variant(c)));
     return FS_OK;
 }
 

@@ -170,45 +170,158 @@ __device__ __forceinline__ u64 plan_product(const Prime& c, const u64* __restric
     return x;
 }
 
-// Walk n over [nstart, nend): test r = n!*R against +-R, then r <- r*(n+1).
-__device__ __forceinline__ u64 walk(u64 r, const Prime& c, u32 nstart, u32 nend, HitStage& st,
-                                    Factor* hits, u32 hitcap, Counters* ctr) {
+// The same for two candidates at once: two independent product chains share
+// every (warp-uniform) table load.
+__device__ __forceinline__ void plan_product2(const Prime& a, const Prime& b, const u64* __restrict__ words,
+                                              const Layer* __restrict__ layers, u32 lb, u32 le, u64& xa,
+                                              u64& xb) {
+    u64 x = a.one, y = b.one;
+    for (u32 l = lb; l < le; ++l) {
+        const Layer L = layers[l];
+        if (l != lb) {
+            x = mont_mul(x, x, a.p, a.pinv);
+            y = mont_mul(y, y, b.p, b.pinv);
+        }
+        if (L.dbl) {
+            x = mod_add(x, x, a.p);
+            y = mod_add(y, y, b.p);
+        }
+        u32 i = L.begin;
+        if ((i & 1) && i < L.end) {
+            const u64 w = __ldg(words + i++);
+            x = mont_mul(x, w, a.p, a.pinv);
+            y = mont_mul(y, w, b.p, b.pinv);
+        }
+        for (; i + 2 <= L.end; i += 2) {
+            const ulonglong2 w2 = __ldg(reinterpret_cast<const ulonglong2*>(words + i));
+            x = mont_mul(x, w2.x, a.p, a.pinv);
+            y = mont_mul(y, w2.x, b.p, b.pinv);
+            x = mont_mul(x, w2.y, a.p, a.pinv);
+            y = mont_mul(y, w2.y, b.p, b.pinv);
+        }
+        if (i < L.end) {
+            const u64 w = __ldg(words + i);
+            x = mont_mul(x, w, a.p, a.pinv);
+            y = mont_mul(y, w, b.p, b.pinv);
+        }
+    }
+    xa = x;
+    xb = y;
+}
+
+struct WalkOut {
+    HitStage* st;
+    Factor* hits;
+    u32 hitcap;
+    Counters* ctr;
+};
+
+// Exact +-1 test of a lazy residue at n, recording a hit.
+__device__ __forceinline__ void lazy_check(u64 r, u32 n, const Lazy64& L, const WalkOut& o) {
+    const u64 c = lazy_canon(r, L);
+    if (c == L.one || c == L.p - L.one)
+        record_hit(*o.st, L.p, c == L.one ? -(int)n : (int)n, o.hits, o.hitcap, o.ctr);
+}
+
+// Replay eight lazy steps from r at n0 with exact tests (the PTX block saw a
+// possible hit in them); the residues are the same bits as the block's.
+__device__ __noinline__ void lazy_replay8(u64 r, u32 n0, const Lazy64& L, WalkOut o) {
+    for (u32 j = 0; j < 8; ++j) {
+        lazy_check(r, n0 + j, L, o);
+        r = lazy_step(r, n0 + j + 1, L);
+    }
+}
+
+// Walk two lazy-eligible candidates over [nstart, nend); residues in and out
+// are canonical.  real_b = false: b duplicates a and its hits are dropped.
+__device__ __forceinline__ void walk_lazy2(u64& ra, u64& rb, const Lazy64& A, const Lazy64& B, bool real_b,
+                                           u32 nstart, u32 nend, const WalkOut& o) {
+    u32 al = (u32)ra, ah = (u32)(ra >> 32), bl = (u32)rb, bh = (u32)(rb >> 32);
+    u32 n = nstart;
+    for (; n + 8 <= nend; n += 8) {
+        const u32 sal = al, sah = ah, sbl = bl, sbh = bh;
+        if (lazy_walk8x2(al, ah, bl, bh, n + 1, A, B)) {
+            lazy_replay8(((u64)sah << 32) | sal, n, A, o);
+            if (real_b) lazy_replay8(((u64)sbh << 32) | sbl, n, B, o);
+        }
+    }
+    u64 a = ((u64)ah << 32) | al, b = ((u64)bh << 32) | bl;
+    for (; n < nend; ++n) {
+        lazy_check(a, n, A, o);
+        a = lazy_step(a, n + 1, A);
+        if (real_b) {
+            lazy_check(b, n, B, o);
+            b = lazy_step(b, n + 1, B);
+        }
+    }
+    ra = lazy_canon(a, A);
+    rb = real_b ? lazy_canon(b, B) : rb;
+}
+
+// Generic walk for any p < 2^64 and n < 2^31: multiply by the Montgomery
+// image of n+1, advanced by R each step (the reference's own step).
+__device__ __forceinline__ u64 walk_generic(u64 r, const Prime& c, u32 nstart, u32 nend, const WalkOut& o) {
     const u64 p = c.p, one = c.one, nmo = p - one;
-    const u32 one_lo = (u32)one, nmo_lo = (u32)nmo;
     if (nstart >= nend) return r;
-    const bool t64 = p > (1ull << 33) && p <= (~0ull) / (u64)nend;
-    if (t64) {
-        const Barrett br = make_barrett(p);
-        u32 n = nstart;
-        for (; n + 4 <= nend; n += 4) {
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const u32 lo = (u32)r;
-                if (lo == one_lo || lo == nmo_lo) {
-                    if (r == one || r == nmo)
-                        record_hit(st, p, r == one ? -(int)(n + j) : (int)(n + j), hits, hitcap, ctr);
-                }
-                r = mul_small_t64(r, n + j + 1, p, br);
-            }
-        }
-        for (; n < nend; ++n) {
-            if (r == one || r == nmo) record_hit(st, p, r == one ? -(int)n : (int)n, hits, hitcap, ctr);
-            r = mul_small_t64(r, n + 1, p, br);
-        }
-    } else {
-        // generic: multiply by the Montgomery image of n+1, advanced by R
-        u64 k = to_mont((u64)nstart + 1, c);
-        for (u32 n = nstart; n < nend; ++n) {
-            if (r == one || r == nmo) record_hit(st, p, r == one ? -(int)n : (int)n, hits, hitcap, ctr);
-            r = mont_mul(r, k, p, c.pinv);
-            k = mod_add(k, one, p);
-        }
+    u64 k = to_mont((u64)nstart + 1, c);
+    for (u32 n = nstart; n < nend; ++n) {
+        if (r == one || r == nmo) record_hit(*o.st, p, r == one ? -(int)n : (int)n, o.hits, o.hitcap, o.ctr);
+        r = mont_mul(r, k, p, c.pinv);
+        k = mod_add(k, one, p);
     }
     return r;
 }
 
-template <int SETUP, bool FINAL>
-__global__ void __launch_bounds__(kSieveThreads) sieve_kernel(SieveArgs a) {
+// Walk both candidates of a pair, choosing the lazy step where it applies.
+__device__ __forceinline__ void walk_pair(u64& ra, u64& rb, const Prime& a, const Prime& b, bool real_b,
+                                          u32 nstart, u32 nend, const WalkOut& o) {
+    if (nstart >= nend) return;
+    const bool la = lazy_ok(a.p, nend), lb = real_b && lazy_ok(b.p, nend);
+    if (la && (lb || !real_b)) {
+        const Lazy64 A = make_lazy(a);
+        const Lazy64 B = real_b ? make_lazy(b) : A;
+        u64 rb2 = real_b ? rb : ra;
+        walk_lazy2(ra, rb2, A, B, real_b, nstart, nend, o);
+        if (real_b) rb = rb2;
+        return;
+    }
+    if (la) {
+        const Lazy64 A = make_lazy(a);
+        u64 dup = ra;
+        walk_lazy2(ra, dup, A, A, false, nstart, nend, o);
+    } else {
+        ra = walk_generic(ra, a, nstart, nend, o);
+    }
+    if (real_b) {
+        if (lb) {
+            const Lazy64 B = make_lazy(b);
+            u64 dup = rb;
+            walk_lazy2(rb, dup, B, B, false, nstart, nend, o);
+        } else {
+            rb = walk_generic(rb, b, nstart, nend, o);
+        }
+    }
+}
+
+// Starting residue of candidate i (SETUP mode), before the walk.
+template <int SETUP>
+__device__ __forceinline__ u64 start_residue_one(const SieveArgs& a, const Prime& c, u32 i) {
+    u64 r;
+    if (SETUP == SETUP_PLAN) {
+        r = plan_product(c, a.plan.words, a.plan.layers, a.plan.layer_begin, a.plan.layer_end);
+        r = mont_mul(r, mont_pow(c.r2, a.plan.deficit, c), c.p, c.pinv);
+    } else if (SETUP == SETUP_PARTIALS) {
+        r = a.partials[i];
+        for (u32 k = 1; k < a.nchunks; ++k) r = mont_mul(r, a.partials[(u64)k * a.cap + i], c.p, c.pinv);
+        r = mont_mul(r, mont_pow(c.r2, a.plan.deficit, c), c.p, c.pinv);
+    } else {
+        r = a.residue[i];
+    }
+    return r;
+}
+
+template <int SETUP, bool FINAL, int MINB>
+__global__ void __launch_bounds__(kSieveThreads, MINB) sieve_kernel(SieveArgs a) {
     __shared__ HitStage st;
     __shared__ u64 wsum[kSieveThreads / 32];
     __shared__ u32 wbad[kSieveThreads / 32];
@@ -216,34 +329,46 @@ __global__ void __launch_bounds__(kSieveThreads) sieve_kernel(SieveArgs a) {
     __syncthreads();
     const u32 ncand = *a.ncand;
     const u32 n = ncand < a.cap ? ncand : a.cap;
+    const WalkOut o{&st, a.hits, a.hitcap, a.ctr};
     u64 sum = 0;
     u32 bad = 0;
+    const u32 npairs = (n + 1) / 2;
     const u32 stride = gridDim.x * blockDim.x;
-    for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const Prime c = make_prime(a.cand[i]);
-        u64 r;
+    for (u32 j = blockIdx.x * blockDim.x + threadIdx.x; j < npairs; j += stride) {
+        const u32 ia = 2 * j, ib = 2 * j + 1;
+        const bool real_b = ib < n;
+        const Prime ca = make_prime(a.cand[ia]);
+        const Prime cb = real_b ? make_prime(a.cand[ib]) : ca;
+        u64 ra, rb;
         if (SETUP == SETUP_PLAN) {
-            r = plan_product(c, a.plan.words, a.plan.layers, a.plan.layer_begin, a.plan.layer_end);
-            r = mont_mul(r, mont_pow(c.r2, a.plan.deficit, c), c.p, c.pinv);
-        } else if (SETUP == SETUP_PARTIALS) {
-            r = a.partials[i];
-            for (u32 k = 1; k < a.nchunks; ++k)
-                r = mont_mul(r, a.partials[(u64)k * a.cap + i], c.p, c.pinv);
-            r = mont_mul(r, mont_pow(c.r2, a.plan.deficit, c), c.p, c.pinv);
+            plan_product2(ca, cb, a.plan.words, a.plan.layers, a.plan.layer_begin, a.plan.layer_end, ra, rb);
+            ra = mont_mul(ra, mont_pow(ca.r2, a.plan.deficit, ca), ca.p, ca.pinv);
+            rb = mont_mul(rb, mont_pow(cb.r2, a.plan.deficit, cb), cb.p, cb.pinv);
         } else {
-            r = a.residue[i];
+            ra = start_residue_one<SETUP>(a, ca, ia);
+            rb = real_b ? start_residue_one<SETUP>(a, cb, ib) : ra;
         }
-        r = walk(r, c, a.nstart, a.nend, st, a.hits, a.hitcap, a.ctr);
+        walk_pair(ra, rb, ca, cb, real_b, a.nstart, a.nend, o);
         if (FINAL) {
             // s7 = nmax*R mod p, the reference's final Montgomery image of n
-            const u64 s7 = to_mont(a.nmax, c);
-            u32 back = (u32)mont_mul(s7, 1, c.p, c.pinv);
-            if (c.p <= a.nmax && a.nmax % c.p == back) back = a.nmax;
-            bad += back != a.nmax;
-            sum += r + s7;
-            if (a.store_final) a.residue[i] = r;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                if (h == 1 && !real_b) break;
+                const Prime& c = h ? cb : ca;
+                const u64 r = h ? rb : ra;
+                const u64 s7 = to_mont(a.nmax, c);
+                u32 back = (u32)mont_mul(s7, 1, c.p, c.pinv);
+                if (c.p <= a.nmax && a.nmax % c.p == back) back = a.nmax;
+                bad += back != a.nmax;
+                sum += r + s7;
+            }
+            if (a.store_final) {
+                a.residue[ia] = ra;
+                if (real_b) a.residue[ib] = rb;
+            }
         } else {
-            a.residue[i] = r;
+            a.residue[ia] = ra;
+            if (real_b) a.residue[ib] = rb;
         }
     }
     if (FINAL) {
@@ -419,17 +544,29 @@ cudaError_t launch_gen(const GenArgs& a, int grid, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_sieve(const SieveArgs& a, int setup, bool final_chunk, int grid, cudaStream_t s) {
+template <int MINB>
+static void launch_sieve_v(const SieveArgs& a, int setup, bool fin, int grid, cudaStream_t s) {
     const int t = kSieveThreads;
     if (setup == SETUP_PLAN) {
-        if (final_chunk) sieve_kernel<SETUP_PLAN, true><<<grid, t, 0, s>>>(a);
-        else sieve_kernel<SETUP_PLAN, false><<<grid, t, 0, s>>>(a);
+        if (fin) sieve_kernel<SETUP_PLAN, true, MINB><<<grid, t, 0, s>>>(a);
+        else sieve_kernel<SETUP_PLAN, false, MINB><<<grid, t, 0, s>>>(a);
     } else if (setup == SETUP_PARTIALS) {
-        if (final_chunk) sieve_kernel<SETUP_PARTIALS, true><<<grid, t, 0, s>>>(a);
-        else sieve_kernel<SETUP_PARTIALS, false><<<grid, t, 0, s>>>(a);
+        if (fin) sieve_kernel<SETUP_PARTIALS, true, MINB><<<grid, t, 0, s>>>(a);
+        else sieve_kernel<SETUP_PARTIALS, false, MINB><<<grid, t, 0, s>>>(a);
     } else {
-        if (final_chunk) sieve_kernel<SETUP_LOAD, true><<<grid, t, 0, s>>>(a);
-        else sieve_kernel<SETUP_LOAD, false><<<grid, t, 0, s>>>(a);
+        if (fin) sieve_kernel<SETUP_LOAD, true, MINB><<<grid, t, 0, s>>>(a);
+        else sieve_kernel<SETUP_LOAD, false, MINB><<<grid, t, 0, s>>>(a);
+    }
+}
+
+// variant v: the kernel compiled for v resident blocks per SM (register cap
+// 65536 / (256 v)); 0 picks the default.
+cudaError_t launch_sieve(const SieveArgs& a, int setup, bool final_chunk, int grid, cudaStream_t s,
+                         int variant) {
+    switch (variant) {
+        case 2: launch_sieve_v<2>(a, setup, final_chunk, grid, s); break;
+        case 4: launch_sieve_v<4>(a, setup, final_chunk, grid, s); break;
+        default: launch_sieve_v<3>(a, setup, final_chunk, grid, s); break;
     }
     return cudaGetLastError();
 }
@@ -453,9 +590,15 @@ cudaError_t launch_imad_bench(u32 iters, u32 kind, u32 seed, u32* sink, int grid
 int sieve_threads() { return kSieveThreads; }
 int gen_threads() { return kGenWarps * 32; }
 
-cudaError_t sieve_occupancy(int* blocks_per_sm) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, sieve_kernel<SETUP_PLAN, true>,
-                                                         kSieveThreads, 0);
+cudaError_t sieve_occupancy(int* blocks_per_sm, int variant) {
+    switch (variant) {
+        case 2: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, sieve_kernel<SETUP_PLAN, true, 2>,
+                                                                     kSieveThreads, 0);
+        case 4: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, sieve_kernel<SETUP_PLAN, true, 4>,
+                                                                     kSieveThreads, 0);
+        default: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, sieve_kernel<SETUP_PLAN, true, 3>,
+                                                                      kSieveThreads, 0);
+    }
 }
 
 }  // namespace fs

@@ -59,11 +59,11 @@ struct TableCheckArgs {
 };
 
 cudaError_t launch_gen(const GenArgs& a, int grid, cudaStream_t s);
-cudaError_t launch_sieve(const SieveArgs& a, int setup, bool final_chunk, int grid, cudaStream_t s);
+cudaError_t launch_sieve(const SieveArgs& a, int setup, bool final_chunk, int grid, cudaStream_t s, int variant);
 cudaError_t launch_setup_partial(const SieveArgs& a, int grid_x, int nchunks, cudaStream_t s);
 cudaError_t launch_table_check(const TableCheckArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_imad_bench(u32 iters, u32 kind, u32 seed, u32* sink, int grid, cudaStream_t s);
-cudaError_t sieve_occupancy(int* blocks_per_sm);
+cudaError_t sieve_occupancy(int* blocks_per_sm, int variant);
 int sieve_threads();
 int gen_threads();
 

@@ -68,6 +68,7 @@ typedef struct {
     uint32_t gen_blocks_per_sm;     /* candidate-generator blocks per SM */
     uint32_t max_steps_per_launch;  /* split the n-range into launches of at most this many steps */
     uint32_t setup_chunks;          /* split the power table across this many threads per prime (1 = never) */
+    uint32_t sieve_variant;         /* sieve kernel build for 2, 3 or 4 resident blocks per SM (register cap) */
 } fs_tuning;
 
 /* ---- library / device ---------------------------------------------------- */
@@ -139,6 +140,20 @@ int fs_table_check(fs_ctx *ctx, const uint64_t *d_cand, fs_counters *d_ctr, uint
                    uint64_t *out2);
 
 /* ---- measurement ---------------------------------------------------------- */
+typedef struct {
+    uint64_t launches;        /* kernels this context launched since the last reset */
+    uint64_t sieve_launches;  /* of which setup/iterate/check kernels */
+    uint64_t gen_launches;    /* of which candidate-generator kernels */
+    double sieve_ms;          /* CUDA-event time of the sieve launches (timing on) */
+    double gen_ms;            /* CUDA-event time of the generator launches (timing on) */
+} fs_stats;
+/* Record CUDA events around every generator and sieve launch on the
+ * context's stream (the reference's profiled enqueue, simpleCL.c:501-550). */
+int fs_set_timing(fs_ctx *ctx, int enable);
+/* Read (and with timing on, wait for) the statistics since the last reset. */
+int fs_get_stats(fs_ctx *ctx, fs_stats *out);
+int fs_reset_stats(fs_ctx *ctx);
+
 /* Dependency-free integer stream on every SM: kind 0 IMAD, 1 IMAD.WIDE,
  * 2 IMAD.HI, 3 LOP3.  Reports warp-lane operations per second. */
 int fs_bench_int_pipe(fs_ctx *ctx, uint32_t kind, uint32_t iters, double *ops_per_sec, double *ms);
