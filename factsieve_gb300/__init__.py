@@ -96,6 +96,7 @@ def _declare(L):
         "fs_reset_stats": (C.c_int, [vp]),
         "fs_power_table": (C.c_int, [u32, P64, P32, P32, u32, P32]),
         "fs_setup_plan": (C.c_int, [u32, u32, P64, u64, P64, P32, u32, P32, P64]),
+        "fs_setup_plan_chunks": (C.c_int, [u32, u32, P32, P64]),
         "fs_find_wheel_offset": (C.c_int, [P64, PI32]),
         "fs_is_prime": (C.c_int, [u64]),
         "fs_verify_factor": (C.c_int, [u64, u32, i32]),
@@ -164,6 +165,16 @@ def setup_plan(n: int, chunks: int = 1):
     if rc:
         raise FSError(rc, "fs_setup_plan")
     return w[:nw.value], lay[:nl.value], d.value
+
+
+def setup_plan_chunks(n: int, chunks: int):
+    """Layer boundaries and deficits of each chunk of the plan for n!."""
+    b = np.zeros(chunks + 1, np.uint32)
+    d = np.zeros(chunks, np.uint64)
+    rc = lib().fs_setup_plan_chunks(n, chunks, _p32(b), _p64(d))
+    if rc:
+        raise FSError(rc, "fs_setup_plan_chunks")
+    return b, d
 
 
 def find_wheel_offset(start: int):

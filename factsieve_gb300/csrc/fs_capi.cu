@@ -774,6 +774,17 @@ int fs_setup_plan(uint32_t n, uint32_t chunks, uint64_t* words, uint64_t wcap, u
     return FS_OK;
 }
 
+int fs_setup_plan_chunks(uint32_t n, uint32_t chunks, uint32_t* bounds, uint64_t* deficits) {
+    if (!bounds || !deficits) return FS_E_ARG;
+    fs::SetupPlan p = fs::build_plan(n, chunks ? chunks : 1);
+    for (size_t i = 0; i < p.chunks.size(); ++i) {
+        bounds[i] = p.chunks[i].layer_begin;
+        deficits[i] = p.chunks[i].deficit;
+    }
+    bounds[p.chunks.size()] = p.chunks.empty() ? 0 : p.chunks.back().layer_end;
+    return FS_OK;
+}
+
 int fs_find_wheel_offset(uint64_t* start, int32_t* index) {
     if (!start || !index) return FS_E_ARG;
     // residues coprime to 30 in wheel order; the gap from res[i] to the next

@@ -166,6 +166,10 @@ int fs_power_table(uint32_t n, uint64_t *prime, uint32_t *exp, uint32_t *bit, ui
  * {begin, end, dbl, 0} quadruples, total R-deficit. */
 int fs_setup_plan(uint32_t n, uint32_t chunks, uint64_t *words, uint64_t wcap, uint64_t *nwords,
                   uint32_t *layers4, uint32_t lcap, uint32_t *nlayers, uint64_t *deficit);
+/* Chunk boundaries of the same plan: chunk c owns layers
+ * [bounds[c], bounds[c+1]) and carries deficits[c] (both arrays chunks+1 /
+ * chunks long). */
+int fs_setup_plan_chunks(uint32_t n, uint32_t chunks, uint32_t *bounds, uint64_t *deficits);
 /* First number >= *start coprime to 30 and its wheel index (cl_sieve.cpp:360-419). */
 int fs_find_wheel_offset(uint64_t *start, int32_t *index);
 /* 7-base deterministic Miller-Rabin (verifyprime.c:105-141). */

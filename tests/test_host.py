@@ -1,0 +1,129 @@
+"""Host-side pieces of libfactsieve.so (no GPU): exported symbols, power table,
+setup plan, CPU factor checks, post-processing, capacity bounds."""
+import math
+import os
+import random
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_library_exports_every_header_symbol(fslib):
+    import ctypes
+    hdr = open(os.path.join(ROOT, "include", "factsieve.h")).read()
+    names = sorted(set(re.findall(r"^\s*(?:const\s+)?[\w\s\*]+?\b(fs_\w+)\s*\(", hdr, re.M)))
+    assert len(names) >= 30
+    raw = ctypes.CDLL(fslib.LIB_PATH)
+    missing = [n for n in names if not hasattr(raw, n)]
+    assert not missing, missing
+
+
+def test_power_table_equals_oracle(fslib, orc):
+    for n in [127, 1000, 54_321, 100_000, 1_000_000]:
+        a = fslib.power_table(n)
+        b = orc.power_table(n)
+        for x, y in zip(a, b):
+            assert x.tolist() == y.tolist(), n
+
+
+@pytest.mark.parametrize("n,chunks", [(127, 1), (1000, 1), (4999, 1), (4999, 3), (20_000, 7), (2, 1), (1, 1)])
+def test_setup_plan_multiplies_to_factorial(fslib, n, chunks):
+    """Horner over each chunk's layers (square, double, multiply words) multiplies to
+    exactly n!, and each chunk's deficit counts one R^-1 per word, doubled by
+    every later squaring -- the bookkeeping the GPU's final correction relies on."""
+    words, layers, deficit = fslib.setup_plan(n, chunks)
+    bounds, deficits = fslib.setup_plan_chunks(n, chunks)
+    total = 1
+    for c in range(chunks):
+        x, d = 1, 0
+        for li in range(int(bounds[c]), int(bounds[c + 1])):
+            b, e, dbl, _ = layers[li].tolist()
+            if li != bounds[c]:
+                x *= x
+                d *= 2
+            if dbl:
+                x *= 2
+            for w in words[b:e].tolist():
+                assert 1 < w < 2**64
+                x *= w
+                d += 1
+        assert d == int(deficits[c])
+        total *= x
+    assert total == math.factorial(n)
+    assert deficit == int(deficits.sum())
+
+
+def test_setup_plan_is_shorter_than_reference_table(fslib):
+    """The bit-layered plan needs fewer Montgomery products per candidate than the
+    reference's table walk (setup.cl:56-102) -- the point of the rewrite."""
+    for n in [100_000, 1_000_000]:
+        words, layers, _ = fslib.setup_plan(n)
+        tp, te, tb = fslib.power_table(n)
+        ref = int(max(int(te[0]), 1).bit_length() - 1)
+        for e in te[1:].tolist():
+            ref += 2 + ((e.bit_length() - 1) + (bin(e).count("1") - 1) if e > 1 else 0)
+        ours = len(words) + len(layers)
+        assert ours * 2.5 < ref, (n, ours, ref)
+
+
+def test_is_prime_and_verify_match_oracle(fslib, orc):
+    rng = random.Random(3)
+    from test_oracle import SPSP2
+    nums = SPSP2 + [127, 65537, 1_000_000_007, (1 << 61) - 1, (1 << 64) - 59] + \
+        [rng.randrange(3, 1 << 64) | 1 for _ in range(2000)]
+    for n in nums:
+        assert fslib.is_prime(n) == orc.is_prime(n), n
+    for _ in range(60):
+        p = rng.randrange(200, 1 << 63) | 1
+        n = rng.randrange(127, 3000)
+        for c in (-1, 1):
+            assert fslib.verify_factor(p, n, c) == orc.verify(p, n, c), (p, n, c)
+
+
+def test_verify_accepts_known_factors(fslib, orc):
+    cand = orc.candidates(127, 2500)
+    hits = orc.sieve_list(cand, 127, 2500)["hits"]
+    assert len(hits) > 50
+    for p, nc in zip(hits["p"].tolist(), hits["nc"].tolist()):
+        assert fslib.verify_factor(p, abs(nc), -1 if nc < 0 else 1)
+        assert not fslib.verify_factor(p, abs(nc), 1 if nc < 0 else -1) or p <= 3
+
+
+def test_postprocess_equals_oracle(fslib, orc):
+    """Sort, verify, 2-PRP filter and n + c checksum equal the oracle's restatement
+    of getResults (cl_sieve.cpp:484-550), including a pseudoprime hit."""
+    cand = np.concatenate([orc.candidates(127, 6000), np.array([2047, 3277], dtype=np.uint64)])
+    hits = orc.sieve_list(cand, 127, 6000)["hits"]
+    rng = np.random.default_rng(5)
+    hits = hits[rng.permutation(len(hits))]
+    kept_o, cs_o, disc_o = orc.postprocess(hits)
+    kept_f, cs_f, disc_f = fslib.postprocess(hits, threads=4)
+    assert cs_f == cs_o
+    assert disc_f == disc_o
+    assert kept_f[["p", "nc"]].tolist() == kept_o[["p", "nc"]].tolist()
+
+
+def test_postprocess_rejects_a_bad_hit(fslib):
+    bad = np.zeros(1, dtype=fslib.FACTOR_DTYPE)
+    bad["p"] = 1_000_003
+    bad["nc"] = 500
+    with pytest.raises(fslib.FSError) as e:
+        fslib.postprocess(bad)
+    assert e.value.code == 7
+
+
+@pytest.mark.parametrize("lo,hi", [(127, 128), (127, 100_000), (1_000_000, 2_000_000), (10**12, 10**12 + 10**6),
+                                   ((1 << 63), (1 << 63) + 10**6), ((1 << 64) - 10**6, (1 << 64) - 1)])
+def test_candidate_capacity_covers_oracle_count(fslib, orc, lo, hi):
+    assert fslib.candidate_capacity(lo, hi) >= len(orc.candidates(lo, hi))
+
+
+def test_context_needs_a_device(fslib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a device is present")
+    with pytest.raises(fslib.FSError):
+        fslib.Context(0)
