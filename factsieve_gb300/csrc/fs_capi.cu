@@ -372,6 +372,7 @@ const char* fs_strerror(int code) {
         case FS_E_VERIFY: return "CPU factor verification failed";
         case FS_E_STATE: return "call out of order";
         case FS_E_TIMEOUT: return "timed out";
+        case FS_E_LIMIT: return "request exceeds a fixed size limit";
         default: return "unknown error";
     }
 }

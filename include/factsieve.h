@@ -34,6 +34,7 @@ extern "C" {
 #define FS_E_VERIFY 7      /* a hit failed CPU verification (cl_sieve.cpp:502-506) */
 #define FS_E_STATE 8       /* call out of order (e.g. segment before begin) */
 #define FS_E_TIMEOUT 9     /* a bounded wait gave up */
+#define FS_E_LIMIT 10      /* request larger than a fixed, compiled-in limit */
 
 /* Factor record, layout of the reference's `factor` (cl_sieve.h:3-6):
  * nc = -n for p | n! - 1, +n for p | n! + 1 (iterate.cl:69-73). */
@@ -183,6 +184,39 @@ int fs_verify_factor(uint64_t p, uint32_t n, int32_t c);
  * any hit fails verification. */
 int fs_postprocess(fs_factor *f, uint64_t n, int threads, uint64_t *kept, uint64_t *checksum_add,
                    uint64_t *discarded);
+
+/* ---- allocation-free segment search ---------------------------------------- */
+/* No counterpart in the reference (it always allocated its buffers with
+ * clCreateBuffer).  For callers that cannot call cudaMalloc -- code running
+ * while a stream is being captured, services whose device memory all comes
+ * from a pool they must not bypass, embedders that only lend preallocated
+ * buffers -- this runs one p-segment [low, high) over n in [nmin, nmax)
+ * exactly like fs_search_begin + fs_search_segment, but allocates nothing:
+ *
+ *   inputs   d_words / d_layers4 / nlayers / deficit: the setup plan for nmin
+ *            as fs_setup_plan() returns it, copied by the caller into device
+ *            memory it owns (layers as {begin, end, dbl, 0} quadruples);
+ *   outputs  d_hits (hitcap records) and d_ctr, caller device memory: hits are
+ *            appended at d_ctr->nhits, sum(s6+s7) added to d_ctr->raw_sum, the
+ *            candidate count to d_ctr->primecount (clear d_ctr before the first
+ *            call of a search, as fs_search_begin does);
+ *   scratch  the candidate list, in a fixed device array of
+ *            FS_NOALLOC_MAX_CANDIDATES entries (8 MiB) that every GPU loading
+ *            this library holds until the process exits.
+ *
+ * A segment whose candidate bound (fs_candidate_capacity) exceeds that
+ * maximum is rejected with FS_E_LIMIT before anything runs; split it.  The
+ * first call on a device, with that device current, looks up the array's
+ * device address and the launch geometry (no allocation); make that first
+ * call before any stream capture.  Work is queued on `stream` (cudaStream_t,
+ * NULL for the legacy default stream) and not waited for.  All calls share
+ * the one array, which keeps the previous call's contents: calls whose work
+ * overlaps on the GPU (other streams, other threads) race on it, so
+ * serialize them. */
+#define FS_NOALLOC_MAX_CANDIDATES (1u << 20)
+int fs_segment_noalloc(uint64_t low, uint64_t high, uint32_t nmin, uint32_t nmax, const uint64_t *d_words,
+                       const uint32_t *d_layers4, uint32_t nlayers, uint64_t deficit, fs_factor *d_hits,
+                       uint32_t hitcap, fs_counters *d_ctr, void *stream);
 
 #ifdef __cplusplus
 }
