@@ -27,8 +27,8 @@ INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["fs_kernels.cu", "fs_capi.cu", "fs_noalloc.cu"]
-CXX_SOURCES = ["fs_host.cpp", "fs_post.cpp"]
-CLI_SOURCES = ["factsieve_main.cpp", "search.cpp", "putil.cpp"]
+CXX_SOURCES = ["fs_host.cpp", "fs_post.cpp", "fs_putil.cpp"]
+CLI_SOURCES = ["factsieve_main.cpp", "search.cpp"]
 
 
 def _nvcc() -> str:

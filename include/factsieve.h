@@ -171,6 +171,11 @@ int fs_setup_plan(uint32_t n, uint32_t chunks, uint64_t *words, uint64_t wcap, u
  * [bounds[c], bounds[c+1]) and carries deficits[c] (both arrays chunks+1 /
  * chunks long). */
 int fs_setup_plan_chunks(uint32_t n, uint32_t chunks, uint32_t *bounds, uint64_t *deficits);
+/* Command-line numbers with the reference's suffixes (putil.c:18-116):
+ * K/M/G/T/P x1000^k, e<d> x10^d, k/m/g/t/p x2^(10k), b<d> x2^d.
+ * 0 ok, -1 unparsable, -2 outside [lo, hi]. */
+int fs_parse_uint64(uint64_t *result, const char *str, uint64_t lo, uint64_t hi);
+int fs_parse_uint(uint32_t *result, const char *str, uint32_t lo, uint32_t hi);
 /* First number >= *start coprime to 30 and its wheel index (cl_sieve.cpp:360-419). */
 int fs_find_wheel_offset(uint64_t *start, int32_t *index);
 /* 7-base deterministic Miller-Rabin (verifyprime.c:105-141). */

@@ -24,6 +24,7 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = os.path.join(_HERE, "liboracle.so")
 _REF = os.path.join(_HERE, "_ref", "libverifyprime.so")
+_REF_PUTIL = os.path.join(_HERE, "_ref", "libputil.so")
 _lock = threading.Lock()
 _lib = None
 _ref = None
@@ -139,6 +140,18 @@ def ref():
         R.verify.argtypes = [u64, u32, C.c_int32]
         _ref = R
     return _ref
+
+
+def ref_putil():
+    """The reference's putil.c (parse_uint64 / parse_uint), or None when not built here."""
+    if not os.path.exists(_REF_PUTIL):
+        return None
+    R = C.CDLL(_REF_PUTIL)
+    R.parse_uint64.restype = C.c_int
+    R.parse_uint64.argtypes = [C.POINTER(C.c_uint64), C.c_char_p, C.c_uint64, C.c_uint64]
+    R.parse_uint.restype = C.c_int
+    R.parse_uint.argtypes = [C.POINTER(C.c_uint32), C.c_char_p, C.c_uint32, C.c_uint32]
+    return R
 
 
 def _p64(a):

@@ -1,0 +1,108 @@
+"""The drop-in CLI on the GPU: factors.txt, checksum line, checkpoint files,
+resume, and the reference's self test."""
+import json
+import os
+import struct
+import subprocess
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _cli(fslib, args, cwd, env=None, timeout=900):
+    if not os.path.exists(fslib.CLI_PATH):
+        pytest.skip("CLI not built")
+    e = dict(os.environ)
+    e.update(env or {})
+    return subprocess.run([fslib.CLI_PATH] + args, cwd=cwd, capture_output=True, text=True, timeout=timeout,
+                          env=e)
+
+
+def _gold(name):
+    with open(os.path.join(GOLD, f"run_{name}.json")) as fh:
+        return json.load(fh)
+
+
+def _state(pmin, pmax, p, checksum, primecount, factorcount, nmin, nmax, last_trickle=0, bad_sum=False):
+    """A 72-byte checkpoint record (cl_sieve.h:9-12) with its additive checksum."""
+    M = (1 << 64) - 1
+    s = (pmin + pmax + p + checksum + primecount + factorcount + last_trickle + nmin + nmax) & M
+    if bad_sum:
+        s ^= 1
+    return struct.pack("<8Q2I", pmin, pmax, p, checksum, primecount, factorcount, last_trickle, s, nmin, nmax)
+
+
+def _args(g):
+    return ["-n", str(g["nmin"]), "-N", str(g["nmax"]), "-p", str(g["pmin"]), "-P", str(g["pmax"]), "-v", "8"]
+
+
+def test_cli_config1_output_files(fslib, tmp_path):
+    g = _gold("config1")
+    r = _cli(fslib, _args(g), tmp_path)
+    assert r.returncode == 0, r.stdout + r.stderr
+    lines = (tmp_path / "factors.txt").read_text().splitlines()
+    assert lines == g["factors"] + [g["checksum"]]
+    assert f"factors {g['factorcount']}, prime count {g['primecount']}, checksum {g['checksum']}" in r.stdout
+    # a checkpoint was written, 72 bytes, finished (p == pmax) and self-consistent
+    ck = [f for f in ("stateA.ckp", "stateB.ckp") if (tmp_path / f).exists()]
+    assert ck
+    rec = (tmp_path / ck[0]).read_bytes()
+    assert len(rec) == 72
+    v = struct.unpack("<8Q2I", rec)
+    assert v[2] == g["pmax"] and v[3] == int(g["checksum"], 16) and v[4] == g["primecount"]
+    assert v[7] == (sum(v[:7]) + v[8] + v[9]) % (1 << 64)
+
+
+def test_cli_no_factors_line(fslib, tmp_path):
+    g = _gold("near_2p62")
+    r = _cli(fslib, _args(g), tmp_path)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert (tmp_path / "factors.txt").read_text().splitlines() == ["no factors", g["checksum"]]
+
+
+def test_cli_resumes_from_checkpoint(fslib, orc, tmp_path):
+    """A checkpoint at p = mid plus the factors found below mid: the resumed run
+    ends with exactly the uninterrupted run's factors.txt and checksum."""
+    g = _gold("config1")
+    mid = 1_500_000
+    part = orc.run(g["pmin"], mid, g["nmin"], g["nmax"])
+    lines = [f"{int(p)} | {abs(int(nc))}!{'+1' if nc > 0 else '-1'}"
+             for p, nc in zip(part["factors"]["p"], part["factors"]["nc"])]
+    (tmp_path / "factors.txt").write_text("".join(l + "\n" for l in lines))
+    (tmp_path / "stateA.ckp").write_bytes(_state(g["pmin"], g["pmax"], mid, part["checksum"], part["primecount"],
+                                                 part["factorcount"], g["nmin"], g["nmax"]))
+    r = _cli(fslib, _args(g), tmp_path)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Resuming from checkpoint in stateA.ckp" in r.stdout
+    assert (tmp_path / "factors.txt").read_text().splitlines() == g["factors"] + [g["checksum"]]
+
+
+def test_cli_ignores_corrupt_checkpoint(fslib, tmp_path):
+    g = _gold("config1")
+    (tmp_path / "stateA.ckp").write_bytes(_state(g["pmin"], g["pmax"], 1_500_000, 5, 7, 0, g["nmin"], g["nmax"],
+                                                 bad_sum=True))
+    (tmp_path / "stateB.ckp").write_bytes(b"short")
+    (tmp_path / "factors.txt").write_text("stale\n")
+    r = _cli(fslib, _args(g), tmp_path)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Checksum error in stateA.ckp" in r.stdout
+    assert "Cannot parse stateB.ckp" in r.stdout
+    assert (tmp_path / "factors.txt").read_text().splitlines() == g["factors"] + [g["checksum"]]
+
+
+def test_cli_finished_workunit(fslib, tmp_path):
+    g = _gold("config1")
+    (tmp_path / "stateB.ckp").write_bytes(_state(g["pmin"], g["pmax"], g["pmax"], 1, 2, 0, g["nmin"], g["nmax"]))
+    r = _cli(fslib, _args(g), tmp_path)
+    assert r.returncode == 0
+    assert "Workunit complete." in r.stdout
+
+
+def test_cli_self_test(fslib, tmp_path):
+    r = _cli(fslib, ["-s", "-v", "16"], tmp_path, timeout=1800)
+    assert r.returncode == 0, r.stdout[-3000:]
+    assert r.stdout.count("passed.") == 5
+    assert "All test cases completed successfully!" in r.stdout
