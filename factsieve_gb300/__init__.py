@@ -51,7 +51,17 @@ class Factor(C.Structure):
 
 class Stats(C.Structure):
     _fields_ = [("launches", C.c_uint64), ("sieve_launches", C.c_uint64), ("gen_launches", C.c_uint64),
-                ("sieve_ms", C.c_double), ("gen_ms", C.c_double)]
+                ("sieve_ms", C.c_double), ("gen_ms", C.c_double), ("batch_launches", C.c_uint64),
+                ("batch_ms", C.c_double)]
+
+
+class Job(C.Structure):
+    _fields_ = [("pmin", C.c_uint64), ("pmax", C.c_uint64), ("nmin", C.c_uint32), ("nmax", C.c_uint32)]
+
+
+class JobResult(C.Structure):
+    _fields_ = [("raw_sum", C.c_uint64), ("primecount", C.c_uint64), ("nhits", C.c_uint64),
+                ("flags", C.c_uint32), ("pad", C.c_uint32)]
 
 
 class Tuning(C.Structure):
@@ -94,6 +104,10 @@ def _declare(L):
         "fs_set_timing": (C.c_int, [vp, C.c_int]),
         "fs_get_stats": (C.c_int, [vp, C.POINTER(Stats)]),
         "fs_reset_stats": (C.c_int, [vp]),
+        "fs_batch_prepare": (C.c_int, [vp, C.POINTER(Job), u32, u32]),
+        "fs_batch_launch": (C.c_int, [vp]),
+        "fs_batch_collect": (C.c_int, [vp, C.POINTER(JobResult), C.POINTER(Factor), u64, P64]),
+        "fs_batch_release": (C.c_int, [vp]),
         "fs_power_table": (C.c_int, [u32, P64, P32, P32, u32, P32]),
         "fs_setup_plan": (C.c_int, [u32, u32, P64, u64, P64, P32, u32, P32, P64]),
         "fs_setup_plan_chunks": (C.c_int, [u32, u32, P32, P64]),
@@ -349,6 +363,47 @@ class Context:
         self._chk(lib().fs_table_check(self._h, C.c_void_p(d_cand), C.c_void_p(d_ctr), nmin, _p64(out)),
                   "fs_table_check")
         return int(out[0]), int(out[1])
+
+    # batches of uneven jobs
+    def batch_prepare(self, jobs, hitcap=1 << 20):
+        """jobs: sequence of (pmin, pmax, nmin, nmax)."""
+        arr = (Job * len(jobs))(*[Job(*map(int, j)) for j in jobs])
+        self._njobs = len(jobs)
+        self._batch_hitcap = hitcap
+        self._chk(lib().fs_batch_prepare(self._h, arr, len(jobs), hitcap), "fs_batch_prepare")
+
+    def batch_launch(self):
+        self._chk(lib().fs_batch_launch(self._h), "fs_batch_launch")
+
+    def batch_collect(self, raise_on_flags=True):
+        """Per-job results (list of dicts) and all hits (pad = job index)."""
+        res = (JobResult * self._njobs)()
+        cap = self._batch_hitcap
+        buf = (Factor * cap)()
+        nh = C.c_uint64(0)
+        rc = lib().fs_batch_collect(self._h, res, buf, cap, C.byref(nh))
+        if rc and raise_on_flags:
+            self._chk(rc, "fs_batch_collect")
+        hits = np.frombuffer(buf, dtype=FACTOR_DTYPE, count=min(nh.value, cap)).copy()
+        out = [{k: getattr(r, k) for k, _ in JobResult._fields_} for r in res]
+        return out, hits, rc
+
+    def batch_release(self):
+        self._chk(lib().fs_batch_release(self._h), "fs_batch_release")
+
+    def batch_sieve(self, jobs, threads=2, hitcap=1 << 20):
+        """Run many jobs in one persistent launch; one SieveResult per job."""
+        self.batch_prepare(jobs, hitcap)
+        self.batch_launch()
+        res, hits, rc = self.batch_collect()
+        out = []
+        for k, r in enumerate(res):
+            mine = hits[hits["pad"] == k].copy()
+            mine["pad"] = 0
+            kept, cs_add, disc = postprocess(mine, threads)
+            out.append(SieveResult(kept, (r["raw_sum"] + cs_add) & 0xFFFFFFFFFFFFFFFF, r["primecount"], len(kept),
+                                   r["raw_sum"], len(mine), disc))
+        return out
 
     # the reference's whole search
     def sieve(self, pmin, pmax, nmin, nmax, threads=2, seg_width=0, result_cap=0) -> SieveResult:

@@ -215,4 +215,206 @@ __device__ __forceinline__ u32 lazy_walk8x2(u32& al, u32& ah, u32& bl, u32& bh, 
     return flag;
 }
 
+// ---------------------------------- iterate: 96-bit Barrett steps --
+//
+// When p k_max > 2^62 the product t = r k needs a third 32-bit word.  The
+// quotient estimate takes 31 bits of t from bit s on, z = floor(t / 2^s),
+// and a 32-bit reciprocal M = floor(2^(32+s) / p):
+//
+//   qe = floor(z M / 2^32),   t/p - z M / 2^32 < 2^s/p + z/2^32 < 1/2 + 1/2,
+//
+// so qe is floor(t/p) or one less, provided k_max < 2^28 (2^s/p <= 2^(kb-29)).
+//
+//   lazy96   p in (2^33, 2^63): r kept in [0, 2p) like the 64-bit lazy step,
+//            s = bitlen(p) + 1 + bitlen(k_max) - 31, r' = (t - qe p) mod 2^64.
+//   canon96  p in [2^63, 2^64): r canonical in [0, p), s = bitlen(p) +
+//            bitlen(k_max) - 31; r' = t - qe p in [0, 2p) needs 65 bits, so
+//            it is formed over three words and folded once.
+
+// floor(2^e / p) for 64 <= e <= 95 and odd p > 1, when it fits 32 bits.
+__device__ __forceinline__ u32 recip_pow2(u64 p, int e) {
+    u64 q = (~0ull) / p;                    // floor(2^64 / p)
+    u64 rem = 0ull - q * p;                 // 2^64 - q p, in [1, p)
+    for (int i = 64; i < e; ++i) {
+        const u64 top = rem >> 63;
+        rem <<= 1;
+        q <<= 1;
+        if (top || rem >= p) {
+            rem -= p;
+            q |= 1;
+        }
+    }
+    return (u32)q;
+}
+
+__device__ __forceinline__ int bitlen64(u64 x) { return 64 - __clzll(x); }
+__device__ __forceinline__ int bitlen32(u32 x) { return 32 - __clz(x); }
+
+struct Lazy96 {
+    u64 p, one;
+    u32 np0, np1, M, sh;      // 2^64 - p, reciprocal, shift s - 32
+    u32 c0, c1, c2, c3;       // low words of one, one + p, p - one, 2p - one
+};
+
+struct Canon96 {
+    u64 p, one;
+    u32 p0, p1, M, sh;
+    u32 c0, c2;               // low words of one and p - one
+};
+
+__device__ __forceinline__ bool lazy96_ok(u64 p, u32 kmax) {
+    return p > (1ull << 33) && (p >> 63) == 0 && bitlen32(kmax) <= 28;
+}
+__device__ __forceinline__ bool canon96_ok(u64 p, u32 kmax) { return (p >> 63) != 0 && bitlen32(kmax) <= 28; }
+
+__device__ __forceinline__ Lazy96 make_lazy96(const Prime& c, u32 kmax) {
+    Lazy96 L;
+    L.p = c.p;
+    L.one = c.one;
+    const u64 np = 0ull - c.p;
+    L.np0 = (u32)np;
+    L.np1 = (u32)(np >> 32);
+    const int s = bitlen64(c.p) + 1 + bitlen32(kmax) - 31;
+    L.sh = (u32)(s - 32);
+    L.M = recip_pow2(c.p, 32 + s);
+    const u64 nmo = c.p - c.one;
+    L.c0 = (u32)c.one;
+    L.c1 = (u32)(c.one + c.p);
+    L.c2 = (u32)nmo;
+    L.c3 = (u32)(nmo + c.p);
+    return L;
+}
+
+__device__ __forceinline__ Canon96 make_canon96(const Prime& c, u32 kmax) {
+    Canon96 C;
+    C.p = c.p;
+    C.one = c.one;
+    C.p0 = (u32)c.p;
+    C.p1 = (u32)(c.p >> 32);
+    const int s = bitlen64(c.p) + bitlen32(kmax) - 31;
+    C.sh = (u32)(s - 32);
+    C.M = recip_pow2(c.p, 32 + s);
+    C.c0 = (u32)c.one;
+    C.c2 = (u32)(c.p - c.one);
+    return C;
+}
+
+// z = bits [32 + sh, 64 + sh) of t = hi:lo, as shf.r.clamp takes them
+__device__ __forceinline__ u32 top_bits(u64 lo, u64 hi, u32 sh) {
+    const u64 t12 = (hi << 32) | (lo >> 32);
+    return (u32)(t12 >> sh);
+}
+
+__device__ __forceinline__ u64 lazy96_step(u64 r, u32 k, const Lazy96& L) {
+    const u64 lo = r * (u64)k, hi = __umul64hi(r, (u64)k);
+    const u32 q = __umulhi(top_bits(lo, hi, L.sh), L.M);
+    return lo + (u64)q * (((u64)L.np1 << 32) | L.np0);
+}
+__device__ __forceinline__ u64 lazy96_canon(u64 r, const Lazy96& L) { return r >= L.p ? r - L.p : r; }
+
+__device__ __forceinline__ u64 canon96_step(u64 r, u32 k, const Canon96& C) {
+    const u64 lo = r * (u64)k, hi = __umul64hi(r, (u64)k);
+    const u32 q = __umulhi(top_bits(lo, hi, C.sh), C.M);
+    const u64 qlo = (u64)q * C.p, qhi = __umul64hi((u64)q, C.p);
+    const u64 rl = lo - qlo;
+    const u64 r2 = hi - qhi - (lo < qlo ? 1ull : 0ull);
+    return (r2 || rl >= C.p) ? rl - C.p : rl;
+}
+
+// Eight lazy96 steps on two residues (operands as lazy_walk8x2 plus shifts).
+#define FS_L96_MUL(RL, RH, NP0, NP1, MM, SH, T, U, R, CC, T0, C, T1, T2, Z, Q)  \
+    "mul.wide.u32 " T ", " RL ", kk;\n\t"                                        \
+    "mov.b64 {" T0 ", " C "}, " T ";\n\t"                                        \
+    "mov.b64 " CC ", {" C ", zr};\n\t"                                           \
+    "mad.wide.u32 " U ", " RH ", kk, " CC ";\n\t"                                \
+    "mov.b64 {" T1 ", " T2 "}, " U ";\n\t"                                       \
+    "shf.r.clamp.b32 " Z ", " T1 ", " T2 ", " SH ";\n\t"                         \
+    "mul.hi.u32 " Q ", " Z ", " MM ";\n\t"                                       \
+    "mov.b64 " T ", {" T0 ", " T1 "};\n\t"                                       \
+    "mad.wide.u32 " R ", " Q ", " NP0 ", " T ";\n\t"                             \
+    "mov.b64 {" RL ", " RH "}, " R ";\n\t"                                       \
+    "mad.lo.u32 " RH ", " Q ", " NP1 ", " RH ";\n\t"
+#define FS_L96_STEP2(J)                                                                        \
+    "add.u32 kk, %5, " #J ";\n\t"                                                              \
+    FS_LZ_TEST("%0", "%10", "%11", "%12", "%13")                                               \
+    FS_LZ_TEST("%2", "%18", "%19", "%20", "%21")                                               \
+    FS_L96_MUL("%0", "%1", "%6", "%7", "%8", "%9", "TA", "UA", "RA", "CA", "a0", "ac", "a1", "a2", "az", "aq") \
+    FS_L96_MUL("%2", "%3", "%14", "%15", "%16", "%17", "TB", "UB", "RB", "CB", "b0", "bc", "b1", "b2", "bz", "bq")
+
+__device__ __forceinline__ u32 lazy96_walk8x2(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const Lazy96& A,
+                                              const Lazy96& B) {
+    u32 flag;
+    asm("{\n\t"
+        ".reg .u32 kk, zr, a0, ac, a1, a2, az, aq, b0, bc, b1, b2, bz, bq;\n\t"
+        ".reg .u64 TA, UA, RA, CA, TB, UB, RB, CB;\n\t"
+        ".reg .pred P;\n\t"
+        "mov.u32 zr, 0;\n\t"
+        "setp.ne.u32 P, %5, %5;\n\t"
+        FS_L96_STEP2(0) FS_L96_STEP2(1) FS_L96_STEP2(2) FS_L96_STEP2(3)
+        FS_L96_STEP2(4) FS_L96_STEP2(5) FS_L96_STEP2(6) FS_L96_STEP2(7)
+        "selp.u32 %4, 1, 0, P;\n\t"
+        "}"
+        : "+r"(al), "+r"(ah), "+r"(bl), "+r"(bh), "=r"(flag)
+        : "r"(k1), "r"(A.np0), "r"(A.np1), "r"(A.M), "r"(A.sh), "r"(A.c0), "r"(A.c1), "r"(A.c2), "r"(A.c3),
+          "r"(B.np0), "r"(B.np1), "r"(B.M), "r"(B.sh), "r"(B.c0), "r"(B.c1), "r"(B.c2), "r"(B.c3));
+    return flag;
+}
+
+// Eight canon96 steps on two residues; the +-1 test needs two compares
+// (canonical residue) and the fold uses a 65-bit comparison.
+#define FS_C96_TEST(RL, C0, C2)                        \
+    "setp.eq.or.u32 P, " RL ", " C0 ", P;\n\t"         \
+    "setp.eq.or.u32 P, " RL ", " C2 ", P;\n\t"
+#define FS_C96_MUL(RL, RH, P0, P1, MM, SH, PP, T, U, A, B, CC, R64, T0, C, T1, T2, Z, Q, X0, X1, Y1, Y2, W2, G) \
+    "mul.wide.u32 " T ", " RL ", kk;\n\t"                                        \
+    "mov.b64 {" T0 ", " C "}, " T ";\n\t"                                        \
+    "mov.b64 " CC ", {" C ", zr};\n\t"                                           \
+    "mad.wide.u32 " U ", " RH ", kk, " CC ";\n\t"                                \
+    "mov.b64 {" T1 ", " T2 "}, " U ";\n\t"                                       \
+    "shf.r.clamp.b32 " Z ", " T1 ", " T2 ", " SH ";\n\t"                         \
+    "mul.hi.u32 " Q ", " Z ", " MM ";\n\t"                                       \
+    "mul.wide.u32 " A ", " Q ", " P0 ";\n\t"                                     \
+    "mov.b64 {" X0 ", " X1 "}, " A ";\n\t"                                       \
+    "mov.b64 " CC ", {" X1 ", zr};\n\t"                                          \
+    "mad.wide.u32 " B ", " Q ", " P1 ", " CC ";\n\t"                             \
+    "mov.b64 {" Y1 ", " Y2 "}, " B ";\n\t"                                       \
+    "sub.cc.u32 " RL ", " T0 ", " X0 ";\n\t"                                     \
+    "subc.cc.u32 " RH ", " T1 ", " Y1 ";\n\t"                                    \
+    "subc.u32 " W2 ", " T2 ", " Y2 ";\n\t"                                       \
+    "mov.b64 " R64 ", {" RL ", " RH "};\n\t"                                     \
+    "setp.ge.u64 " G ", " R64 ", " PP ";\n\t"                                    \
+    "setp.ne.or.u32 " G ", " W2 ", 0, " G ";\n\t"                                \
+    "@" G " sub.cc.u32 " RL ", " RL ", " P0 ";\n\t"                              \
+    "@" G " subc.u32 " RH ", " RH ", " P1 ";\n\t"
+#define FS_C96_STEP2(J)                                                                                 \
+    "add.u32 kk, %5, " #J ";\n\t"                                                                       \
+    FS_C96_TEST("%0", "%10", "%11")                                                                     \
+    FS_C96_TEST("%2", "%16", "%17")                                                                     \
+    FS_C96_MUL("%0", "%1", "%6", "%7", "%8", "%9", "PA", "TA", "UA", "AA", "BA", "CA", "RA", "a0", "ac", "a1", \
+               "a2", "az", "aq", "ax0", "ax1", "ay1", "ay2", "aw", "GA")                                \
+    FS_C96_MUL("%2", "%3", "%12", "%13", "%14", "%15", "PB", "TB", "UB", "AB", "BB", "CB", "RB", "b0", "bc", "b1", \
+               "b2", "bz", "bq", "bx0", "bx1", "by1", "by2", "bw", "GB")
+
+__device__ __forceinline__ u32 canon96_walk8x2(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const Canon96& A,
+                                               const Canon96& B) {
+    u32 flag;
+    asm("{\n\t"
+        ".reg .u32 kk, zr, a0, ac, a1, a2, az, aq, ax0, ax1, ay1, ay2, aw;\n\t"
+        ".reg .u32 b0, bc, b1, b2, bz, bq, bx0, bx1, by1, by2, bw;\n\t"
+        ".reg .u64 TA, UA, AA, BA, CA, RA, PA, TB, UB, AB, BB, CB, RB, PB;\n\t"
+        ".reg .pred P, GA, GB;\n\t"
+        "mov.u32 zr, 0;\n\t"
+        "mov.b64 PA, {%6, %7};\n\t"
+        "mov.b64 PB, {%12, %13};\n\t"
+        "setp.ne.u32 P, %5, %5;\n\t"
+        FS_C96_STEP2(0) FS_C96_STEP2(1) FS_C96_STEP2(2) FS_C96_STEP2(3)
+        FS_C96_STEP2(4) FS_C96_STEP2(5) FS_C96_STEP2(6) FS_C96_STEP2(7)
+        "selp.u32 %4, 1, 0, P;\n\t"
+        "}"
+        : "+r"(al), "+r"(ah), "+r"(bl), "+r"(bh), "=r"(flag)
+        : "r"(k1), "r"(A.p0), "r"(A.p1), "r"(A.M), "r"(A.sh), "r"(A.c0), "r"(A.c2),
+          "r"(B.p0), "r"(B.p1), "r"(B.M), "r"(B.sh), "r"(B.c0), "r"(B.c2));
+    return flag;
+}
+
 }  // namespace fs

@@ -68,6 +68,27 @@ struct fs_ctx {
     int chk_grid = 0;
     u32* d_sink = nullptr;
     std::map<std::pair<uint32_t, uint32_t>, PlanGPU> plans;
+    // batch
+    struct Batch {
+        bool ready = false;
+        uint32_t njobs = 0;
+        std::vector<uint32_t> order;        // device slot k runs caller job order[k]
+        std::vector<uint64_t> cap;          // candidate capacity per slot
+        u64* d_cand = nullptr;
+        u64* d_words = nullptr;
+        fs::Layer* d_layers = nullptr;
+        fs::BatchJob* d_jobs = nullptr;
+        fs::Counters* d_ctr = nullptr;      // per slot
+        fs::Counters* d_gctr = nullptr;     // batch-wide
+        u32* d_tile = nullptr;
+        fs::Factor* d_hits = nullptr;
+        uint32_t hitcap = 0;
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+    } batch;
+    uint64_t batch_launches = 0;
+    double batch_ms = 0;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> batch_ev;
     // statistics
     bool timing = false;
     uint64_t launches = 0, sieve_launches = 0, gen_launches = 0;
@@ -117,13 +138,13 @@ int ev_end(fs_ctx* c, std::pair<cudaEvent_t, cudaEvent_t>& ev, std::vector<std::
 }
 
 int ev_drain(fs_ctx* c) {
-    for (int k = 0; k < 2; ++k) {
-        auto& list = k ? c->gen_ev : c->sieve_ev;
+    for (int k = 0; k < 3; ++k) {
+        auto& list = k == 2 ? c->batch_ev : k ? c->gen_ev : c->sieve_ev;
         for (auto& ev : list) {
             CK(c, cudaEventSynchronize(ev.second));
             float ms = 0;
             CK(c, cudaEventElapsedTime(&ms, ev.first, ev.second));
-            (k ? c->gen_ms : c->sieve_ms) += ms;
+            (k == 2 ? c->batch_ms : k ? c->gen_ms : c->sieve_ms) += ms;
             c->ev_pool.push_back(ev);
         }
         list.clear();
@@ -442,7 +463,8 @@ int fs_destroy(fs_ctx* c) {
     cudaFree(c->d_chk_done);
     cudaFree(c->d_chk_result);
     cudaFree(c->d_sink);
-    for (auto* l : {&c->sieve_ev, &c->gen_ev, &c->ev_pool})
+    fs_batch_release(c);
+    for (auto* l : {&c->sieve_ev, &c->gen_ev, &c->batch_ev, &c->ev_pool})
         for (auto& ev : *l) {
             cudaEventDestroy(ev.first);
             cudaEventDestroy(ev.second);
@@ -468,6 +490,8 @@ int fs_get_stats(fs_ctx* c, fs_stats* out) {
     out->gen_launches = c->gen_launches;
     out->sieve_ms = c->sieve_ms;
     out->gen_ms = c->gen_ms;
+    out->batch_launches = c->batch_launches;
+    out->batch_ms = c->batch_ms;
     return FS_OK;
 }
 
@@ -476,8 +500,8 @@ int fs_reset_stats(fs_ctx* c) {
     int rc = bind(c);
     if (rc) return rc;
     if ((rc = ev_drain(c))) return rc;
-    c->launches = c->sieve_launches = c->gen_launches = 0;
-    c->sieve_ms = c->gen_ms = 0;
+    c->launches = c->sieve_launches = c->gen_launches = c->batch_launches = 0;
+    c->sieve_ms = c->gen_ms = c->batch_ms = 0;
     return FS_OK;
 }
 
@@ -805,3 +829,218 @@ int fs_is_prime(uint64_t p) { return fs::is_prime_u64(p) ? 1 : 0; }
 int fs_verify_factor(uint64_t p, uint32_t n, int32_t c) { return fs::verify_factor(p, n, c) ? 1 : 0; }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ batch --
+
+namespace {
+
+// Work per candidate of a job in walk-step units: the walk (slower steps for
+// larger p*k) plus the setup (about 0.036 n Montgomery products, each worth
+// about 2.7 walk steps).
+double job_cost(const fs_job& j) {
+    const double w = (double)(j.nmax - j.nmin);
+    const double pk = (double)j.pmax * (double)j.nmax;
+    const double wf = pk <= 4.6e18 ? 1.0 : (j.pmax < (1ull << 63) ? 1.2 : 1.5);
+    return w * wf + 0.036 * (double)j.nmin * 2.7 + 64.0;
+}
+
+void batch_free(fs_ctx* c) {
+    auto& b = c->batch;
+    if (b.exec) cudaGraphExecDestroy(b.exec);
+    if (b.graph) cudaGraphDestroy(b.graph);
+    cudaFree(b.d_cand);
+    cudaFree(b.d_words);
+    cudaFree(b.d_layers);
+    cudaFree(b.d_jobs);
+    cudaFree(b.d_ctr);
+    cudaFree(b.d_gctr);
+    cudaFree(b.d_tile);
+    cudaFree(b.d_hits);
+    b = fs_ctx::Batch();
+}
+
+}  // namespace
+
+extern "C" int fs_batch_release(fs_ctx* c) {
+    if (!c) return FS_E_ARG;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    batch_free(c);
+    return FS_OK;
+}
+
+extern "C" int fs_batch_prepare(fs_ctx* c, const fs_job* jobs, uint32_t njobs, uint32_t hitcap) {
+    if (!c || !jobs || njobs == 0 || njobs > (uint32_t)fs::batch_max_jobs() || hitcap == 0) return FS_E_ARG;
+    for (uint32_t i = 0; i < njobs; ++i) {
+        const fs_job& j = jobs[i];
+        if (j.nmin > j.nmax || j.nmax > 0x7FFFFFFFu || j.pmin > j.pmax || j.pmin < j.nmin || j.pmin < 3) {
+            c->err = "invalid job " + std::to_string(i);
+            return FS_E_ARG;
+        }
+        if (fs_candidate_capacity(j.pmin, j.pmax) >= 0xFFFFFFF0ull || (j.pmax - j.pmin) / 64 >= (1ull << 31)) {
+            c->err = "job " + std::to_string(i) + " too wide";
+            return FS_E_ARG;
+        }
+    }
+    int rc = bind(c);
+    if (rc) return rc;
+    CK(c, cudaStreamSynchronize(c->stream));
+    batch_free(c);
+    auto& b = c->batch;
+    b.njobs = njobs;
+    b.order.resize(njobs);
+    for (uint32_t i = 0; i < njobs; ++i) b.order[i] = i;
+    std::stable_sort(b.order.begin(), b.order.end(),
+                     [&](uint32_t x, uint32_t y) { return job_cost(jobs[x]) > job_cost(jobs[y]); });
+    // plans: one per distinct nmin, concatenated
+    std::map<uint32_t, std::pair<uint32_t, uint32_t>> layer_range;   // nmin -> [begin, end)
+    std::map<uint32_t, uint64_t> deficit;
+    std::vector<uint64_t> words;
+    std::vector<fs::Layer> layers;
+    for (uint32_t i = 0; i < njobs; ++i) {
+        const uint32_t n = jobs[i].nmin;
+        if (layer_range.count(n)) continue;
+        fs::SetupPlan p = fs::build_plan(n, 1);
+        const uint32_t woff = (uint32_t)words.size(), lb = (uint32_t)layers.size();
+        words.insert(words.end(), p.words.begin(), p.words.end());
+        if (words.size() & 1) words.push_back(0);   // keep every plan's paired loads 16-byte aligned
+        for (const auto& L : p.layers) layers.push_back({L.begin + woff, L.end + woff, L.dbl, 0});
+        layer_range[n] = {lb, (uint32_t)layers.size()};
+        deficit[n] = p.deficit;
+    }
+    std::vector<fs::BatchJob> dj(njobs);
+    b.cap.resize(njobs);
+    uint64_t total = 0;
+    std::vector<uint64_t> off(njobs);
+    for (uint32_t k = 0; k < njobs; ++k) {
+        const fs_job& j = jobs[b.order[k]];
+        b.cap[k] = fs_candidate_capacity(j.pmin, j.pmax);
+        off[k] = total;
+        total += (b.cap[k] + 1) & ~1ull;
+    }
+    CK(c, cudaMalloc((void**)&b.d_cand, (total + 2) * sizeof(u64)));
+    CK(c, cudaMalloc((void**)&b.d_words, (words.size() + 2) * sizeof(u64)));
+    CK(c, cudaMalloc((void**)&b.d_layers, (layers.size() + 1) * sizeof(fs::Layer)));
+    CK(c, cudaMalloc((void**)&b.d_jobs, njobs * sizeof(fs::BatchJob)));
+    CK(c, cudaMalloc((void**)&b.d_ctr, njobs * sizeof(fs::Counters)));
+    CK(c, cudaMalloc((void**)&b.d_gctr, sizeof(fs::Counters)));
+    CK(c, cudaMalloc((void**)&b.d_tile, sizeof(u32)));
+    CK(c, cudaMalloc((void**)&b.d_hits, (size_t)hitcap * sizeof(fs::Factor)));
+    b.hitcap = hitcap;
+    for (uint32_t k = 0; k < njobs; ++k) {
+        const fs_job& j = jobs[b.order[k]];
+        dj[k].cand = b.d_cand + off[k];
+        dj[k].cap = (u32)b.cap[k];
+        dj[k].nstart = j.nmin;
+        dj[k].nend = j.nmax;
+        dj[k].layer_begin = layer_range[j.nmin].first;
+        dj[k].layer_end = layer_range[j.nmin].second;
+        dj[k].pad = 0;
+        dj[k].deficit = deficit[j.nmin];
+    }
+    CK(c, cudaMemcpy(b.d_words, words.data(), words.size() * sizeof(u64), cudaMemcpyHostToDevice));
+    CK(c, cudaMemcpy(b.d_layers, layers.data(), layers.size() * sizeof(fs::Layer), cudaMemcpyHostToDevice));
+    CK(c, cudaMemcpy(b.d_jobs, dj.data(), njobs * sizeof(fs::BatchJob), cudaMemcpyHostToDevice));
+    int occ = 0;
+    if (fs::batch_occupancy(&occ) != cudaSuccess || occ < 1) occ = 1;
+
+    // capture: clears, the candidate launches, the persistent sieve
+    CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaMemsetAsync(b.d_ctr, 0, njobs * sizeof(fs::Counters), c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b.d_gctr, 0, sizeof(fs::Counters), c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b.d_tile, 0, sizeof(u32), c->stream);
+    const bool timing = c->timing;
+    const uint64_t l0 = c->launches, g0 = c->gen_launches;
+    c->timing = false;   // no event records inside the capture
+    int grc = FS_OK;
+    for (uint32_t k = 0; k < njobs && e == cudaSuccess && grc == FS_OK; ++k) {
+        const fs_job& j = jobs[b.order[k]];
+        grc = run_gen(c, j.pmin, j.pmax, b.d_cand + off[k], (uint32_t)b.cap[k], b.d_ctr + k);
+    }
+    c->timing = timing;
+    c->launches = l0;    // launches are counted when the graph replays
+    c->gen_launches = g0;
+    fs::BatchArgs a;
+    memset(&a, 0, sizeof(a));
+    a.jobs = b.d_jobs;
+    a.njobs = njobs;
+    a.ctr = b.d_ctr;
+    a.gctr = b.d_gctr;
+    a.tile_counter = b.d_tile;
+    a.words = b.d_words;
+    a.layers = b.d_layers;
+    a.hits = b.d_hits;
+    a.hitcap = hitcap;
+    if (e == cudaSuccess && grc == FS_OK) e = fs::launch_batch(a, c->sm_count * occ, c->stream);
+    cudaGraph_t g = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+    if (grc != FS_OK) {
+        if (g) cudaGraphDestroy(g);
+        return grc;
+    }
+    CK(c, e);
+    CK(c, e2);
+    b.graph = g;
+    CK(c, cudaGraphInstantiate(&b.exec, g, 0));
+    b.ready = true;
+    return FS_OK;
+}
+
+extern "C" int fs_batch_launch(fs_ctx* c) {
+    if (!c) return FS_E_ARG;
+    if (!c->batch.ready) return FS_E_STATE;
+    int rc = bind(c);
+    if (rc) return rc;
+    std::pair<cudaEvent_t, cudaEvent_t> ev;
+    if ((rc = ev_begin(c, &ev))) return rc;
+    CK(c, cudaGraphLaunch(c->batch.exec, c->stream));
+    if ((rc = ev_end(c, ev, c->batch_ev))) return rc;
+    c->launches += c->batch.njobs + 1;
+    c->gen_launches += c->batch.njobs;
+    ++c->batch_launches;
+    return FS_OK;
+}
+
+extern "C" int fs_batch_collect(fs_ctx* c, fs_job_result* results, fs_factor* hits, uint64_t hitcap,
+                                uint64_t* nhits) {
+    if (!c) return FS_E_ARG;
+    auto& b = c->batch;
+    if (!b.ready) return FS_E_STATE;
+    int rc = bind(c);
+    if (rc) return rc;
+    std::vector<fs::Counters> h(b.njobs);
+    fs::Counters g;
+    CK(c, cudaStreamSynchronize(c->stream));
+    CK(c, cudaMemcpy(h.data(), b.d_ctr, b.njobs * sizeof(fs::Counters), cudaMemcpyDeviceToHost));
+    CK(c, cudaMemcpy(&g, b.d_gctr, sizeof(g), cudaMemcpyDeviceToHost));
+    const uint64_t stored = std::min<uint64_t>(g.nhits, b.hitcap);
+    std::vector<fs::Factor> hv(stored);
+    if (stored) CK(c, cudaMemcpy(hv.data(), b.d_hits, stored * sizeof(fs::Factor), cudaMemcpyDeviceToHost));
+    uint32_t any = g.flags;
+    std::vector<uint64_t> per(b.njobs, 0);
+    for (auto& f : hv) {
+        const uint32_t k = (uint32_t)f.pad;
+        f.pad = (int)b.order[k];
+        per[k]++;
+    }
+    for (uint32_t k = 0; k < b.njobs; ++k) {
+        uint32_t fl = h[k].flags;
+        if (h[k].ncand > b.cap[k]) fl |= FS_FLAG_CAND_OVERFLOW;
+        any |= fl;
+        if (results) {
+            fs_job_result& r = results[b.order[k]];
+            r.raw_sum = h[k].raw_sum;
+            r.primecount = h[k].ncand;
+            r.nhits = per[k];
+            r.flags = fl;
+            r.pad = 0;
+        }
+    }
+    if (nhits) *nhits = g.nhits;
+    if (hits) memcpy(hits, hv.data(), std::min<uint64_t>(stored, hitcap) * sizeof(fs_factor));
+    if (any & FS_FLAG_TABLE) return FS_E_TABLE;
+    if (any & FS_FLAG_VALIDATION) return FS_E_VALIDATION;
+    if ((any & (FS_FLAG_CAND_OVERFLOW | FS_FLAG_HIT_OVERFLOW)) || g.nhits > b.hitcap || (hits && g.nhits > hitcap))
+        return FS_E_OVERFLOW;
+    return FS_OK;
+}

@@ -124,7 +124,7 @@ struct HitStage {
 // shared-memory stage with one shared atomic (warp-ballot compaction); a full
 // stage spills straight to the global list.
 __device__ __noinline__ void record_hit(HitStage& st, u64 p, int nc, Factor* hits, u32 hitcap,
-                                        Counters* ctr) {
+                                        Counters* ctr, int tag) {
     const u32 mask = __activemask();
     const int lane = threadIdx.x & 31;
     const int leader = __ffs(mask) - 1;
@@ -136,13 +136,13 @@ __device__ __noinline__ void record_hit(HitStage& st, u64 p, int nc, Factor* hit
     if (slot < kHitStage) {
         st.buf[slot].p = p;
         st.buf[slot].nc = nc;
-        st.buf[slot].pad = 0;
+        st.buf[slot].pad = tag;
     } else {
         u32 g = atomicAdd(&ctr->nhits, 1u);
         if (g < hitcap) {
             hits[g].p = p;
             hits[g].nc = nc;
-            hits[g].pad = 0;
+            hits[g].pad = tag;
         } else {
             atomicOr(&ctr->flags, FLAG_HIT_OVERFLOW);
         }
@@ -214,48 +214,91 @@ struct WalkOut {
     Factor* hits;
     u32 hitcap;
     Counters* ctr;
+    int tag;   // stored in each hit record's pad word (job index in a batch, else 0)
 };
 
-// Exact +-1 test of a lazy residue at n, recording a hit.
-__device__ __forceinline__ void lazy_check(u64 r, u32 n, const Lazy64& L, const WalkOut& o) {
-    const u64 c = lazy_canon(r, L);
-    if (c == L.one || c == L.p - L.one)
-        record_hit(*o.st, L.p, c == L.one ? -(int)n : (int)n, o.hits, o.hitcap, o.ctr);
+// The three Barrett walk regimes behind one interface.
+struct RegT64 {
+    using K = Lazy64;
+    static __device__ __forceinline__ K make(const Prime& c, u32) { return make_lazy(c); }
+    static __device__ __forceinline__ u32 block(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const K& A, const K& B) {
+        return lazy_walk8x2(al, ah, bl, bh, k1, A, B);
+    }
+    static __device__ __forceinline__ u64 step(u64 r, u32 k, const K& X) { return lazy_step(r, k, X); }
+    static __device__ __forceinline__ u64 canon(u64 r, const K& X) { return lazy_canon(r, X); }
+};
+struct RegL96 {
+    using K = Lazy96;
+    static __device__ __forceinline__ K make(const Prime& c, u32 kmax) { return make_lazy96(c, kmax); }
+    static __device__ __forceinline__ u32 block(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const K& A, const K& B) {
+        return lazy96_walk8x2(al, ah, bl, bh, k1, A, B);
+    }
+    static __device__ __forceinline__ u64 step(u64 r, u32 k, const K& X) { return lazy96_step(r, k, X); }
+    static __device__ __forceinline__ u64 canon(u64 r, const K& X) { return lazy96_canon(r, X); }
+};
+struct RegC96 {
+    using K = Canon96;
+    static __device__ __forceinline__ K make(const Prime& c, u32 kmax) { return make_canon96(c, kmax); }
+    static __device__ __forceinline__ u32 block(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const K& A, const K& B) {
+        return canon96_walk8x2(al, ah, bl, bh, k1, A, B);
+    }
+    static __device__ __forceinline__ u64 step(u64 r, u32 k, const K& X) { return canon96_step(r, k, X); }
+    static __device__ __forceinline__ u64 canon(u64 r, const K&) { return r; }
+};
+
+// Exact +-1 test of a walk residue at n, recording a hit.
+template <class Reg>
+__device__ __forceinline__ void reg_check(u64 r, u32 n, const typename Reg::K& X, const WalkOut& o) {
+    const u64 c = Reg::canon(r, X);
+    if (c == X.one || c == X.p - X.one)
+        record_hit(*o.st, X.p, c == X.one ? -(int)n : (int)n, o.hits, o.hitcap, o.ctr, o.tag);
 }
 
-// Replay eight lazy steps from r at n0 with exact tests (the PTX block saw a
+// Replay eight steps from r at n0 with exact tests (the PTX block saw a
 // possible hit in them); the residues are the same bits as the block's.
-__device__ __noinline__ void lazy_replay8(u64 r, u32 n0, const Lazy64& L, WalkOut o) {
+template <class Reg>
+__device__ __noinline__ void reg_replay8(u64 r, u32 n0, typename Reg::K X, WalkOut o) {
     for (u32 j = 0; j < 8; ++j) {
-        lazy_check(r, n0 + j, L, o);
-        r = lazy_step(r, n0 + j + 1, L);
+        reg_check<Reg>(r, n0 + j, X, o);
+        r = Reg::step(r, n0 + j + 1, X);
     }
 }
 
-// Walk two lazy-eligible candidates over [nstart, nend); residues in and out
+// Walk two candidates of one regime over [nstart, nend); residues in and out
 // are canonical.  real_b = false: b duplicates a and its hits are dropped.
-__device__ __forceinline__ void walk_lazy2(u64& ra, u64& rb, const Lazy64& A, const Lazy64& B, bool real_b,
-                                           u32 nstart, u32 nend, const WalkOut& o) {
+template <class Reg>
+__device__ __forceinline__ void walk_reg2(u64& ra, u64& rb, const typename Reg::K& A, const typename Reg::K& B,
+                                          bool real_b, u32 nstart, u32 nend, const WalkOut& o) {
     u32 al = (u32)ra, ah = (u32)(ra >> 32), bl = (u32)rb, bh = (u32)(rb >> 32);
     u32 n = nstart;
     for (; n + 8 <= nend; n += 8) {
         const u32 sal = al, sah = ah, sbl = bl, sbh = bh;
-        if (lazy_walk8x2(al, ah, bl, bh, n + 1, A, B)) {
-            lazy_replay8(((u64)sah << 32) | sal, n, A, o);
-            if (real_b) lazy_replay8(((u64)sbh << 32) | sbl, n, B, o);
+        if (Reg::block(al, ah, bl, bh, n + 1, A, B)) {
+            reg_replay8<Reg>(((u64)sah << 32) | sal, n, A, o);
+            if (real_b) reg_replay8<Reg>(((u64)sbh << 32) | sbl, n, B, o);
         }
     }
     u64 a = ((u64)ah << 32) | al, b = ((u64)bh << 32) | bl;
     for (; n < nend; ++n) {
-        lazy_check(a, n, A, o);
-        a = lazy_step(a, n + 1, A);
+        reg_check<Reg>(a, n, A, o);
+        a = Reg::step(a, n + 1, A);
         if (real_b) {
-            lazy_check(b, n, B, o);
-            b = lazy_step(b, n + 1, B);
+            reg_check<Reg>(b, n, B, o);
+            b = Reg::step(b, n + 1, B);
         }
     }
-    ra = lazy_canon(a, A);
-    rb = real_b ? lazy_canon(b, B) : rb;
+    ra = Reg::canon(a, A);
+    if (real_b) rb = Reg::canon(b, B);
+}
+
+template <class Reg>
+__device__ __forceinline__ void walk_reg_pair(u64& ra, u64& rb, const Prime& a, const Prime& b, bool real_b,
+                                              u32 nstart, u32 nend, const WalkOut& o) {
+    const typename Reg::K A = Reg::make(a, nend);
+    const typename Reg::K B = real_b ? Reg::make(b, nend) : A;
+    u64 rb2 = real_b ? rb : ra;
+    walk_reg2<Reg>(ra, rb2, A, B, real_b, nstart, nend, o);
+    if (real_b) rb = rb2;
 }
 
 // Generic walk for any p < 2^64 and n < 2^31: multiply by the Montgomery
@@ -265,42 +308,47 @@ __device__ __forceinline__ u64 walk_generic(u64 r, const Prime& c, u32 nstart, u
     if (nstart >= nend) return r;
     u64 k = to_mont((u64)nstart + 1, c);
     for (u32 n = nstart; n < nend; ++n) {
-        if (r == one || r == nmo) record_hit(*o.st, p, r == one ? -(int)n : (int)n, o.hits, o.hitcap, o.ctr);
+        if (r == one || r == nmo) record_hit(*o.st, p, r == one ? -(int)n : (int)n, o.hits, o.hitcap, o.ctr, o.tag);
         r = mont_mul(r, k, p, c.pinv);
         k = mod_add(k, one, p);
     }
     return r;
 }
 
-// Walk both candidates of a pair, choosing the lazy step where it applies.
+// Walk regime of one candidate for multipliers up to kmax: 1 lazy 64-bit,
+// 2 lazy 96-bit, 3 canonical 96-bit, 0 generic Montgomery.
+__device__ __forceinline__ int walk_regime(u64 p, u32 kmax) {
+    if (lazy_ok(p, kmax)) return 1;
+    if (lazy96_ok(p, kmax)) return 2;
+    if (canon96_ok(p, kmax)) return 3;
+    return 0;
+}
+
+__device__ __forceinline__ void walk_one(u64& r, const Prime& c, int reg, u32 nstart, u32 nend, const WalkOut& o) {
+    u64 dup = r;
+    switch (reg) {
+        case 1: walk_reg_pair<RegT64>(r, dup, c, c, false, nstart, nend, o); break;
+        case 2: walk_reg_pair<RegL96>(r, dup, c, c, false, nstart, nend, o); break;
+        case 3: walk_reg_pair<RegC96>(r, dup, c, c, false, nstart, nend, o); break;
+        default: r = walk_generic(r, c, nstart, nend, o); break;
+    }
+}
+
+// Walk both candidates of a pair, each with the fastest step that applies.
 __device__ __forceinline__ void walk_pair(u64& ra, u64& rb, const Prime& a, const Prime& b, bool real_b,
                                           u32 nstart, u32 nend, const WalkOut& o) {
     if (nstart >= nend) return;
-    const bool la = lazy_ok(a.p, nend), lb = real_b && lazy_ok(b.p, nend);
-    if (la && (lb || !real_b)) {
-        const Lazy64 A = make_lazy(a);
-        const Lazy64 B = real_b ? make_lazy(b) : A;
-        u64 rb2 = real_b ? rb : ra;
-        walk_lazy2(ra, rb2, A, B, real_b, nstart, nend, o);
-        if (real_b) rb = rb2;
-        return;
-    }
-    if (la) {
-        const Lazy64 A = make_lazy(a);
-        u64 dup = ra;
-        walk_lazy2(ra, dup, A, A, false, nstart, nend, o);
-    } else {
-        ra = walk_generic(ra, a, nstart, nend, o);
-    }
-    if (real_b) {
-        if (lb) {
-            const Lazy64 B = make_lazy(b);
-            u64 dup = rb;
-            walk_lazy2(rb, dup, B, B, false, nstart, nend, o);
-        } else {
-            rb = walk_generic(rb, b, nstart, nend, o);
+    const int ga = walk_regime(a.p, nend);
+    const int gb = real_b ? walk_regime(b.p, nend) : ga;
+    if (ga == gb && ga != 0) {
+        switch (ga) {
+            case 1: walk_reg_pair<RegT64>(ra, rb, a, b, real_b, nstart, nend, o); return;
+            case 2: walk_reg_pair<RegL96>(ra, rb, a, b, real_b, nstart, nend, o); return;
+            default: walk_reg_pair<RegC96>(ra, rb, a, b, real_b, nstart, nend, o); return;
         }
     }
+    walk_one(ra, a, ga, nstart, nend, o);
+    if (real_b) walk_one(rb, b, gb, nstart, nend, o);
 }
 
 // Starting residue of candidate i (SETUP mode), before the walk.
@@ -329,7 +377,7 @@ __global__ void __launch_bounds__(kSieveThreads, MINB) sieve_kernel(SieveArgs a)
     __syncthreads();
     const u32 ncand = *a.ncand;
     const u32 n = ncand < a.cap ? ncand : a.cap;
-    const WalkOut o{&st, a.hits, a.hitcap, a.ctr};
+    const WalkOut o{&st, a.hits, a.hitcap, a.ctr, 0};
     u64 sum = 0;
     u32 bad = 0;
     const u32 npairs = (n + 1) / 2;
@@ -426,6 +474,112 @@ __global__ void __launch_bounds__(kSieveThreads) setup_partial_kernel(SieveArgs 
         const Prime c = make_prime(a.cand[i]);
         a.partials[(u64)chunk * a.cap + i] =
             plan_product(c, a.plan.words, a.plan.layers, pc.layer_begin, pc.layer_end);
+    }
+}
+
+// ============================================================ batches ====
+
+// Persistent kernel over many uneven jobs.  A tile is 2 x blockDim candidates
+// of one job; blocks take tiles from a global counter until the batch is
+// done.  The host orders jobs by estimated work per candidate, heaviest
+// first, so the long tiles start early and the tail is made of short ones.
+constexpr int kBatchMaxJobs = 1024;
+
+__global__ void __launch_bounds__(kSieveThreads, 3) batch_sieve_kernel(BatchArgs a) {
+    __shared__ HitStage st;
+    __shared__ u32 tile_end[kBatchMaxJobs];   // inclusive prefix sum of tiles per job
+    __shared__ u32 s_tile;
+    __shared__ u64 wsum[kSieveThreads / 32];
+    __shared__ u32 wbad[kSieveThreads / 32];
+    const u32 per_tile = 2 * blockDim.x;
+    if (threadIdx.x == 0) {
+        st.n = 0;
+        u32 acc = 0;
+        for (u32 j = 0; j < a.njobs; ++j) {
+            const u32 nc = a.ctr[j].ncand;
+            const u32 n = nc < a.jobs[j].cap ? nc : a.jobs[j].cap;
+            acc += (n + per_tile - 1) / per_tile;
+            tile_end[j] = acc;
+        }
+    }
+    __syncthreads();
+    const u32 total = tile_end[a.njobs - 1];
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(a.tile_counter, 1u);
+        __syncthreads();
+        const u32 t = s_tile;
+        __syncthreads();
+        if (t >= total) break;
+        // job of tile t: first j with tile_end[j] > t (binary search)
+        u32 lo = 0, hi = a.njobs - 1;
+        while (lo < hi) {
+            const u32 mid = (lo + hi) >> 1;
+            if (tile_end[mid] > t) hi = mid;
+            else lo = mid + 1;
+        }
+        const u32 j = lo;
+        const BatchJob& J = a.jobs[j];
+        const u32 nc = a.ctr[j].ncand;
+        const u32 n = nc < J.cap ? nc : J.cap;
+        const u32 first = (t - (j ? tile_end[j - 1] : 0)) * per_tile;
+        const u32 ia = first + 2 * threadIdx.x, ib = ia + 1;
+        u64 sum = 0;
+        u32 bad = 0;
+        if (ia < n) {
+            const WalkOut o{&st, a.hits, a.hitcap, a.gctr, (int)j};
+            const bool real_b = ib < n;
+            const Prime ca = make_prime(J.cand[ia]);
+            const Prime cb = real_b ? make_prime(J.cand[ib]) : ca;
+            u64 ra, rb;
+            plan_product2(ca, cb, a.words, a.layers, J.layer_begin, J.layer_end, ra, rb);
+            ra = mont_mul(ra, mont_pow(ca.r2, J.deficit, ca), ca.p, ca.pinv);
+            rb = mont_mul(rb, mont_pow(cb.r2, J.deficit, cb), cb.p, cb.pinv);
+            walk_pair(ra, rb, ca, cb, real_b, J.nstart, J.nend, o);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                if (h == 1 && !real_b) break;
+                const Prime& c = h ? cb : ca;
+                const u64 s7 = to_mont(J.nend, c);
+                u32 back = (u32)mont_mul(s7, 1, c.p, c.pinv);
+                if (c.p <= J.nend && J.nend % c.p == back) back = J.nend;
+                bad += back != J.nend;
+                sum += (h ? rb : ra) + s7;
+            }
+        }
+#pragma unroll
+        for (int d = 16; d; d >>= 1) {
+            sum += __shfl_xor_sync(0xffffffffu, sum, d);
+            bad += __shfl_xor_sync(0xffffffffu, bad, d);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            wsum[threadIdx.x >> 5] = sum;
+            wbad[threadIdx.x >> 5] = bad;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            u64 s = 0;
+            u32 b = 0;
+            for (int w = 0; w < (int)(blockDim.x / 32); ++w) {
+                s += wsum[w];
+                b += wbad[w];
+            }
+            if (s) atomicAdd(&a.ctr[j].raw_sum, s);
+            if (b) atomicOr(&a.ctr[j].flags, FLAG_VALIDATION);
+        }
+    }
+    __syncthreads();
+    const u32 nh = st.n < kHitStage ? st.n : kHitStage;
+    if (nh) {
+        __shared__ u32 gbase;
+        if (threadIdx.x == 0) gbase = atomicAdd(&a.gctr->nhits, nh);
+        __syncthreads();
+        for (u32 k = threadIdx.x; k < nh; k += blockDim.x) {
+            const u32 g = gbase + k;
+            if (g < a.hitcap)
+                a.hits[g] = st.buf[k];
+            else
+                atomicOr(&a.gctr->flags, FLAG_HIT_OVERFLOW);
+        }
     }
 }
 
@@ -576,6 +730,18 @@ cudaError_t launch_setup_partial(const SieveArgs& a, int grid_x, int nchunks, cu
     setup_partial_kernel<<<g, kSieveThreads, 0, s>>>(a);
     return cudaGetLastError();
 }
+
+cudaError_t launch_batch(const BatchArgs& a, int grid, cudaStream_t s) {
+    if (a.njobs == 0 || a.njobs > (u32)kBatchMaxJobs) return cudaErrorInvalidValue;
+    batch_sieve_kernel<<<grid, kSieveThreads, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t batch_occupancy(int* blocks_per_sm) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, batch_sieve_kernel, kSieveThreads, 0);
+}
+
+int batch_max_jobs() { return kBatchMaxJobs; }
 
 cudaError_t launch_table_check(const TableCheckArgs& a, int grid, cudaStream_t s) {
     table_check_kernel<<<grid, 256, 0, s>>>(a);

@@ -58,7 +58,32 @@ struct TableCheckArgs {
     Counters* ctr;
 };
 
+// One job of a batch: its candidates, n-range and setup-plan layers.
+struct BatchJob {
+    const u64* cand;
+    u32 cap;
+    u32 nstart, nend;            // walk [nstart, nend); s7 = nend * R
+    u32 layer_begin, layer_end;  // its plan's layers in the shared layer table
+    u32 pad;
+    u64 deficit;
+};
+
+struct BatchArgs {
+    const BatchJob* jobs;
+    u32 njobs;
+    Counters* ctr;               // per job: ncand (from the generator), raw_sum, flags
+    Counters* gctr;              // batch-wide: nhits, overflow flags
+    u32* tile_counter;           // zeroed before each run
+    const u64* words;
+    const Layer* layers;
+    Factor* hits;                // pad = job index
+    u32 hitcap;
+};
+
 cudaError_t launch_gen(const GenArgs& a, int grid, cudaStream_t s);
+cudaError_t launch_batch(const BatchArgs& a, int grid, cudaStream_t s);
+cudaError_t batch_occupancy(int* blocks_per_sm);
+int batch_max_jobs();
 cudaError_t launch_sieve(const SieveArgs& a, int setup, bool final_chunk, int grid, cudaStream_t s, int variant);
 cudaError_t launch_setup_partial(const SieveArgs& a, int grid_x, int nchunks, cudaStream_t s);
 cudaError_t launch_table_check(const TableCheckArgs& a, int grid, cudaStream_t s);

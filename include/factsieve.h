@@ -113,6 +113,37 @@ int fs_search_range(fs_ctx *ctx, uint64_t low, uint64_t high, uint64_t seg_width
 /* Capacity the context reserves for one segment of the given width. */
 uint64_t fs_candidate_capacity(uint64_t low, uint64_t high);
 
+/* ---- batches of uneven jobs (one persistent launch) ------------------------ */
+typedef struct {
+    uint64_t pmin, pmax;   /* p in [pmin, pmax) */
+    uint32_t nmin, nmax;   /* n in [nmin, nmax) */
+} fs_job;
+
+typedef struct {
+    uint64_t raw_sum;      /* sum of (s6 + s7) over the job's candidates, mod 2^64 */
+    uint64_t primecount;   /* candidates of the job */
+    uint64_t nhits;        /* hits of the job before the 2-PRP filter */
+    uint32_t flags;        /* FS_FLAG_* of the job */
+    uint32_t pad;
+} fs_job_result;
+
+/* Prepare a batch: build every job's setup plan, size its candidate buffer
+ * and capture the whole batch -- counter clears, one candidate launch per job
+ * and one persistent sieve launch whose blocks take (job, 512-candidate) tiles
+ * from a global queue, heaviest jobs first -- into a CUDA graph.  Replaces any
+ * previous batch of the context.  Each job's results are bit-identical to a
+ * search of that job alone.  No counterpart in the reference, which runs one
+ * range per process. */
+int fs_batch_prepare(fs_ctx *ctx, const fs_job *jobs, uint32_t njobs, uint32_t hitcap);
+/* Replay the batch graph on the context's stream (asynchronous). */
+int fs_batch_launch(fs_ctx *ctx);
+/* Wait, then copy per-job results (in the caller's job order) and the hits;
+ * each hit's pad word holds its job index.  Returns FS_E_OVERFLOW or
+ * FS_E_VALIDATION when a job flagged one. */
+int fs_batch_collect(fs_ctx *ctx, fs_job_result *results, fs_factor *hits, uint64_t hitcap, uint64_t *nhits);
+/* Free the batch's device memory and graph. */
+int fs_batch_release(fs_ctx *ctx);
+
 /* ---- stage-level kernels on caller device buffers ------------------------ */
 /* getsegprimes (getsegprimes.cl:170-239): append the candidates of
  * [low, high) to d_cand at slot d_ctr->ncand (the reference's
@@ -147,6 +178,8 @@ typedef struct {
     uint64_t gen_launches;    /* of which candidate-generator kernels */
     double sieve_ms;          /* CUDA-event time of the sieve launches (timing on) */
     double gen_ms;            /* CUDA-event time of the generator launches (timing on) */
+    uint64_t batch_launches;  /* batch graph replays */
+    double batch_ms;          /* CUDA-event time of the batch graph replays (timing on) */
 } fs_stats;
 /* Record CUDA events around every generator and sieve launch on the
  * context's stream (the reference's profiled enqueue, simpleCL.c:501-550). */

@@ -192,3 +192,60 @@ def test_hit_overflow_is_reported(ctx):
     hits, raw, pc, flags, rc = ctx.collect(10, raise_on_flags=False)
     assert rc == fs.FS_E_OVERFLOW
     assert flags & fs.FLAG_HIT_OVERFLOW
+
+
+@pytest.mark.parametrize("lo,hi,nmin,nmax", [
+    (10**15, 10**15 + 300_000, 100_000, 100_700),                  # lazy 96-bit step (p < 2^63, p k > 2^62)
+    ((1 << 63) + 1, (1 << 63) + 300_000, 5_000, 5_700),             # canonical 96-bit step (p >= 2^63)
+    ((1 << 64) - 400_000, (1 << 64) - 1, 1_000, 1_333),              # canonical 96-bit step near 2^64
+    (4 * 10**12, 4 * 10**12 + 200_000, 1_000_000, 1_000_300),      # across the 64/96-bit boundary
+])
+def test_walk_regimes_match_oracle(ctx, orc, lo, hi, nmin, nmax):
+    """Every walk regime (and a pair straddling two) gives the oracle's residues, sums and hits."""
+    import factsieve_gb300 as fs
+    want_c = orc.candidates(lo, hi)
+    cap = fs.candidate_capacity(lo, hi)
+    cand, res, hits, ctr = _dev_buffers(cap)
+    ctx.getsegprimes(lo, hi, cand.data_ptr(), cap, ctr.data_ptr())
+    ctx.setup(cand.data_ptr(), cap, ctr.data_ptr(), nmin, res.data_ptr())
+    ctx.iterate(cand.data_ptr(), cap, ctr.data_ptr(), res.data_ptr(), nmin, nmax, hits.data_ptr(), 1 << 16)
+    ctx.check(cand.data_ptr(), cap, ctr.data_ptr(), res.data_ptr(), nmax)
+    ctx.synchronize()
+    c = _counters(ctr)
+    n = int(c["ncand"])
+    got_c = _u64(cand)[:n]
+    order = np.argsort(got_c)
+    assert got_c[order].tolist() == want_c.tolist()
+    want = orc.sieve_list(want_c, nmin, nmax, want_residues=True)
+    assert _u64(res)[:n][order].tolist() == want["s6"].tolist()
+    assert int(c["raw_sum"]) == want["raw_sum"]
+    assert int(c["flags"]) == 0
+    assert _sorted_hits(_hits_array(hits, int(c["nhits"]))) == _sorted_hits(want["hits"])
+
+
+def test_walk_with_multipliers_beyond_2p28(ctx, orc):
+    """n above 2^28 takes the generic Montgomery walk; still bit-exact."""
+    import factsieve_gb300 as fs
+    nmin, nmax = (1 << 28) + 5, (1 << 28) + 200
+    lo, hi = 10**12, 10**12 + 400
+    want_c = orc.candidates(lo, hi)
+    assert len(want_c) >= 4
+    cap = fs.candidate_capacity(lo, hi)
+    cand, res, hits, ctr = _dev_buffers(cap)
+    ctx.getsegprimes(lo, hi, cand.data_ptr(), cap, ctr.data_ptr())
+    ctx.setup(cand.data_ptr(), cap, ctr.data_ptr(), nmin, res.data_ptr())
+    ctx.iterate(cand.data_ptr(), cap, ctr.data_ptr(), res.data_ptr(), nmin, nmax, hits.data_ptr(), 1 << 16)
+    ctx.check(cand.data_ptr(), cap, ctr.data_ptr(), res.data_ptr(), nmax)
+    ctx.synchronize()
+    c = _counters(ctr)
+    want = orc.sieve_list(want_c, nmin, nmax)
+    assert int(c["raw_sum"]) == want["raw_sum"]
+    assert int(c["flags"]) == 0
+
+
+@pytest.mark.parametrize("name", ["config3_slice100", "config2_slice100", "selftest1"])
+def test_search_matches_long_fixture(ctx, name):
+    g = _golden(name)
+    r = ctx.sieve(g["pmin"], g["pmax"], g["nmin"], g["nmax"], threads=16)
+    assert (r.primecount, f"{r.raw_sum:016X}", f"{r.checksum:016X}", r.factorcount) == \
+        (g["primecount"], g["raw_sum"], g["checksum"], g["factorcount"])
