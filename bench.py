@@ -50,6 +50,7 @@ WORKLOADS = {
     "config3": (1 << 63, (1 << 63) + 1_000_000_000, 1_000_000, 1_010_000, 100_000_000),
 }
 IMAD_PER_PRODUCT = 20   # reference m_mul on 32-bit limbs (8 mul_wide + 4 + 8)
+GOLDEN = os.path.join(ROOT, "tests", "golden")
 
 
 # ------------------------------------------------------------ helpers -----
@@ -328,19 +329,161 @@ def run_ours(args):
     return 0
 
 
+def load_jobs():
+    with open(os.path.join(GOLDEN, "jobs_config4.json")) as fh:
+        return [tuple(j) for j in json.load(fh)["jobs"]]
+
+
+def run_batch(args):
+    """Config 4: 64 uneven jobs (seed 1) in one persistent, graph-captured
+    launch against the same 64 jobs run one after another through the plain
+    path on the same GPU.  Both legs are timed with CUDA events on the
+    library's stream (device time) and with the wall clock; every job's
+    (primecount, raw sum, hits) must agree between the legs."""
+    import torch
+    import factsieve_gb300 as fs
+    jobs = load_jobs()
+    dev = torch.cuda.current_device()
+    ctx = fs.Context(dev)
+    stream = torch.cuda.Stream(device=dev)
+    ctx.set_stream(stream.cuda_stream)
+    cap = 1 << 20
+    small = [(p0, p0 + max(10_000, (p1 - p0) // 200), n0, n1) for p0, p1, n0, n1 in jobs]
+    for _ in range(args.warmup):                  # warm-up: the same mix at 1/200 of the p-widths
+        ctx.batch_sieve(small)
+    # batched leg
+    ctx.batch_prepare(jobs, hitcap=cap)
+    ctx.reset_stats()
+    ctx.set_timing(True)
+    torch.cuda.synchronize(dev)
+    with ClockSampler(dev) as clk:
+        t0 = time.perf_counter()
+        ctx.batch_launch()
+        res, hits, rc = ctx.batch_collect()
+        wall_b = time.perf_counter() - t0
+    st = ctx.stats()
+    ctx.set_timing(False)
+    assert rc == 0
+    dev_b = st["batch_ms"] * 1e-3
+    pairs = sum(r["primecount"] * (j[3] - j[2]) for r, j in zip(res, jobs))
+    ctx.batch_release()
+    # plain leg: 64 sequential searches
+    ctx.reset_stats()
+    ctx.set_timing(True)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    plain = []
+    for j in jobs:
+        ctx.begin(*j)
+        ctx.run_range(j[0], j[1])
+        h, raw, pc, flags, rc2 = ctx.collect(cap)
+        assert rc2 == 0
+        plain.append((pc, raw, sorted(zip(h["p"].tolist(), h["nc"].tolist()))))
+    wall_p = time.perf_counter() - t0
+    sp = ctx.stats()
+    ctx.set_timing(False)
+    dev_p = (sp["sieve_ms"] + sp["gen_ms"]) * 1e-3
+    same = True
+    for k, (r, pl) in enumerate(zip(res, plain)):
+        mine = sorted(zip(hits["p"][hits["pad"] == k].tolist(), hits["nc"][hits["pad"] == k].tolist()))
+        same &= (r["primecount"], r["raw_sum"], mine) == pl
+    line = {
+        "metric": "(p,n) pair-steps/sec", "value": pairs / dev_b, "unit": "pair-steps/s", "n_gpus": 1,
+        "steps": 1, "warmup": args.warmup, "ms_per_step": dev_b * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic (64 jobs, seed 1)",
+        "config": {"workload": "config4: 64 uneven jobs in one persistent launch (tests/golden/jobs_config4.json)",
+                   "warmup": "the same 64 jobs at 1/200 of their p-widths", "pair_steps": pairs},
+        "batched": {"device_s": dev_b, "wall_s": wall_b, "pair_steps_per_s": pairs / dev_b,
+                    "wall_pair_steps_per_s": pairs / wall_b},
+        "plain_sequential": {"device_s": dev_p, "wall_s": wall_p, "pair_steps_per_s": pairs / dev_p,
+                             "wall_pair_steps_per_s": pairs / wall_p},
+        "speedup_device": dev_p / dev_b, "speedup_wall": wall_p / wall_b,
+        "per_job_bit_exact": bool(same),
+        "gpu_launches": int(st["launches"]),
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0
+
+
+def run_serve(args):
+    """Config 5: the seed-2 Poisson stream (20 requests/s for 120 s, job sizes
+    from the config-4 distribution) replayed in real time through the serving
+    loop, reporting served versus offered load and p50/p99 sojourn time.  The
+    offered load is far above one GPU, so a second, explicitly labelled run
+    replays the same arrivals with every p-width divided by 1000."""
+    import math
+    import torch
+    import factsieve_gb300 as fs
+    from factsieve_gb300.serve import run_stream
+    with open(os.path.join(GOLDEN, "stream_config5.json")) as fh:
+        reqs = [tuple(r) for r in json.load(fh)["requests"]]
+    dev = torch.cuda.current_device()
+    ctx = fs.Context(dev)
+
+    def est_pairs(r):
+        p0, p1, n0, n1 = r[1:5] if len(r) == 5 else r
+        return (p1 - p0) / math.log(p0) * (n1 - n0)
+
+    # warm-up: three short streams
+    small = [(t * 0.01, p0, p0 + max(10_000, (p1 - p0) // 2000), n0, n1) for t, p0, p1, n0, n1 in reqs[:20]]
+    for _ in range(args.warmup):
+        run_stream(ctx, small, stop_after_s=30)
+    with ClockSampler(dev) as clk:
+        full, done_full = run_stream(ctx, reqs, stop_after_s=args.serve_seconds, max_active=16,
+                                     pair_steps_of=est_pairs)
+    scaled = [(t, p0, p0 + max(10_000, (p1 - p0) // 1000), n0, n1) for t, p0, p1, n0, n1 in reqs]
+    small_sum, done_small = run_stream(ctx, scaled, stop_after_s=args.serve_seconds, max_active=16,
+                                       pair_steps_of=est_pairs)
+    # bit-exactness of a sample of finished jobs against the same job alone
+    sample = sorted(done_small)[:: max(1, len(done_small) // 8)][:8]
+    exact = True
+    for k in sample:
+        d = done_small[k]
+        _, p0, p1, n0, n1 = scaled[k]
+        a = ctx.sieve(p0, p1, n0, n1, threads=os.cpu_count() or 2)
+        kept, cs_add, _ = fs.postprocess(d["hits"], threads=os.cpu_count() or 2)
+        exact &= (d["primecount"], (d["raw_sum"] + cs_add) & 0xFFFFFFFFFFFFFFFF) == (a.primecount, a.checksum)
+    line = {
+        "metric": "(p,n) pair-steps/sec", "value": full["served_pair_steps_per_s"], "unit": "pair-steps/s",
+        "n_gpus": 1, "steps": 1, "warmup": args.warmup, "ms_per_step": full["elapsed_s"] * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic (Poisson stream, seed 2)",
+        "config": {"workload": "config5: Poisson 20 req/s for 120 s, config-4 job sizes, continuous batching",
+                   "stop_after_s": args.serve_seconds, "max_active": 16},
+        "served": full,
+        "offered_vs_served": {"offered_pair_steps_per_s_est": full.get("offered_pair_steps_per_s"),
+                              "served_pair_steps_per_s": full["served_pair_steps_per_s"]},
+        "latency_s": {"p50": full["p50_s"], "p99": full["p99_s"], "note": "sojourn (arrival to result) of "
+                      "completed requests; the stream overloads one GPU, so later requests are still queued"},
+        "scaled_down_stream": dict(small_sum, label="same arrivals, every p-width divided by 1000"),
+        "per_job_bit_exact_sample": {"jobs": len(sample), "exact": bool(exact)},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS) + ["config4", "config5"])
+    ap.add_argument("--serve-seconds", type=float, default=180.0, help="config5: stop the replay after this long")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "config4":
+        return run_batch(args)
+    if args.workload == "config5":
+        return run_serve(args)
     return run_ours(args)
 
 

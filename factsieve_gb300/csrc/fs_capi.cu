@@ -18,6 +18,7 @@
 
 #include "../../include/factsieve.h"
 #include "fs_host.h"
+#include "fs_internal.h"
 #include "fs_launch.h"
 
 static_assert(sizeof(fs_factor) == 16, "factor record is 16 bytes");
@@ -29,83 +30,11 @@ namespace {
 constexpr u32 kQ[29] = {3,  5,  7,  11, 13, 17, 19, 23, 29,  31,  37,  41,  43,  47, 53,
                         59, 61, 67, 71, 73, 79, 83, 89, 97, 101, 103, 107, 109, 113};
 
-struct PlanGPU {
-    uint32_t n = 0, nchunks = 0;
-    u64* d_words = nullptr;
-    fs::Layer* d_layers = nullptr;
-    fs::PlanChunkDev* d_chunks = nullptr;
-    uint64_t deficit = 0, nwords = 0;
-    uint32_t nlayers = 0;
-    std::vector<fs::PlanChunkDev> chunks;
-};
+using fs_internal::PlanGPU;
 
 }  // namespace
 
-struct fs_ctx {
-    int device = 0;
-    cudaStream_t own = nullptr, stream = nullptr;
-    int sm_count = 0, clock_khz = 0;
-    uint64_t total_mem = 0;
-    int sieve_occ[5] = {1, 1, 1, 1, 1};
-    fs_tuning tuning{};
-    std::string err;
-    // search state
-    bool active = false, table_checked = false;
-    uint64_t pmin = 0, pmax = 0;
-    uint32_t nmin = 0, nmax = 0;
-    fs::Counters* d_ctr = nullptr;
-    u64* d_cand = nullptr;
-    uint64_t cand_cap = 0;
-    u64* d_residue = nullptr;
-    uint64_t residue_cap = 0;
-    u64* d_partials = nullptr;
-    uint64_t partials_cap = 0;
-    fs::Factor* d_hits = nullptr;
-    uint32_t hit_cap = 0;
-    u64* d_chk_scratch = nullptr;
-    u32* d_chk_done = nullptr;
-    u64* d_chk_result = nullptr;
-    int chk_grid = 0;
-    u32* d_sink = nullptr;
-    std::map<std::pair<uint32_t, uint32_t>, PlanGPU> plans;
-    // batch
-    struct Batch {
-        bool ready = false;
-        uint32_t njobs = 0;
-        std::vector<uint32_t> order;        // device slot k runs caller job order[k]
-        std::vector<uint64_t> cap;          // candidate capacity per slot
-        u64* d_cand = nullptr;
-        u64* d_words = nullptr;
-        fs::Layer* d_layers = nullptr;
-        fs::BatchJob* d_jobs = nullptr;
-        fs::Counters* d_ctr = nullptr;      // per slot
-        fs::Counters* d_gctr = nullptr;     // batch-wide
-        u32* d_tile = nullptr;
-        fs::Factor* d_hits = nullptr;
-        uint32_t hitcap = 0;
-        cudaGraph_t graph = nullptr;
-        cudaGraphExec_t exec = nullptr;
-    } batch;
-    uint64_t batch_launches = 0;
-    double batch_ms = 0;
-    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> batch_ev;
-    // statistics
-    bool timing = false;
-    uint64_t launches = 0, sieve_launches = 0, gen_launches = 0;
-    double sieve_ms = 0, gen_ms = 0;
-    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> sieve_ev, gen_ev, ev_pool;
-};
-
-#define CK(ctx, call)                                                          \
-    do {                                                                       \
-        cudaError_t e_ = (call);                                               \
-        if (e_ != cudaSuccess) {                                               \
-            (ctx)->err = std::string(#call) + ": " + cudaGetErrorString(e_);   \
-            return e_ == cudaErrorMemoryAllocation ? FS_E_NOMEM : FS_E_CUDA;   \
-        }                                                                      \
-    } while (0)
-
-namespace {
+namespace fs_internal {
 
 int bind(fs_ctx* c) {
     cudaError_t e = cudaSetDevice(c->device);
@@ -115,6 +44,12 @@ int bind(fs_ctx* c) {
     }
     return FS_OK;
 }
+
+}  // namespace fs_internal
+
+namespace {
+
+using fs_internal::bind;
 
 // A pair of events around one launch when timing is on.
 int ev_begin(fs_ctx* c, std::pair<cudaEvent_t, cudaEvent_t>* ev) {
@@ -248,7 +183,9 @@ uint32_t auto_chunks(fs_ctx* c, uint64_t est_cand, uint32_t n) {
     return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(k, 64));
 }
 
-int run_gen(fs_ctx* c, uint64_t low, uint64_t high, u64* d_cand, uint32_t cap, fs::Counters* d_ctr) {
+}  // namespace
+
+int fs_internal::run_gen(fs_ctx* c, uint64_t low, uint64_t high, u64* d_cand, uint32_t cap, fs::Counters* d_ctr) {
     if (high <= low) return FS_OK;
     uint64_t o0 = low | 1ull;
     if (o0 < low || o0 >= high) return FS_OK;
@@ -276,6 +213,10 @@ int run_gen(fs_ctx* c, uint64_t low, uint64_t high, u64* d_cand, uint32_t cap, f
     ++c->gen_launches;
     return ev_end(c, ev, c->gen_ev);
 }
+
+namespace {
+
+using fs_internal::run_gen;
 
 int run_table_check(fs_ctx* c, const u64* d_cand, fs::Counters* d_ctr, uint32_t n, PlanGPU* pl) {
     if (!c->d_chk_scratch) {
@@ -464,6 +405,7 @@ int fs_destroy(fs_ctx* c) {
     cudaFree(c->d_chk_result);
     cudaFree(c->d_sink);
     fs_batch_release(c);
+    fs_serve_destroy(c);
     for (auto* l : {&c->sieve_ev, &c->gen_ev, &c->batch_ev, &c->ev_pool})
         for (auto& ev : *l) {
             cudaEventDestroy(ev.first);

@@ -583,6 +583,112 @@ __global__ void __launch_bounds__(kSieveThreads, 3) batch_sieve_kernel(BatchArgs
     }
 }
 
+// ============================================================ serving ====
+
+// One round of the serving loop: a list of tiles, each up to 2 x blockDim
+// candidates of one job in one phase (starting residue from the plan, a
+// chunk of the walk, the final checksum), taken from a global counter by
+// persistent blocks.  Residues live in each job's device buffer between
+// rounds.
+__global__ void __launch_bounds__(kSieveThreads, 3) serve_round_kernel(ServeArgs a) {
+    __shared__ HitStage st;
+    __shared__ u32 s_tile;
+    __shared__ u64 wsum[kSieveThreads / 32];
+    __shared__ u32 wbad[kSieveThreads / 32];
+    if (threadIdx.x == 0) st.n = 0;
+    __syncthreads();
+    const u32 per_tile = 2 * blockDim.x;
+    const u32 ntiles = a.nchunks ? a.chunks[a.nchunks - 1].tile_end : 0;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(a.tile_counter, 1u);
+        __syncthreads();
+        const u32 t = s_tile;
+        __syncthreads();
+        if (t >= ntiles) break;
+        // chunk of tile t: first c with tile_end > t
+        u32 lo = 0, hi = a.nchunks - 1;
+        while (lo < hi) {
+            const u32 mid = (lo + hi) >> 1;
+            if (a.chunks[mid].tile_end > t) hi = mid;
+            else lo = mid + 1;
+        }
+        const ServeChunk T = a.chunks[lo];
+        const u32 tile0 = lo ? a.chunks[lo - 1].tile_end : 0;
+        const u32 first = T.first + (t - tile0) * per_tile;
+        const u32 ia = first + 2 * threadIdx.x, ib = ia + 1;
+        const u32 end = T.first + T.count;
+        u64 sum = 0;
+        u32 bad = 0;
+        if (ia < end) {
+            const WalkOut o{&st, a.hits, a.hitcap, a.gctr, (int)T.tag};
+            const bool real_b = ib < end;
+            const Prime ca = make_prime(T.cand[ia]);
+            const Prime cb = real_b ? make_prime(T.cand[ib]) : ca;
+            u64 ra, rb;
+            if (T.flags & SERVE_SETUP) {
+                plan_product2(ca, cb, T.words, T.layers, T.layer_begin, T.layer_end, ra, rb);
+                ra = mont_mul(ra, mont_pow(ca.r2, T.deficit, ca), ca.p, ca.pinv);
+                rb = mont_mul(rb, mont_pow(cb.r2, T.deficit, cb), cb.p, cb.pinv);
+            } else {
+                ra = T.residue[ia];
+                rb = real_b ? T.residue[ib] : ra;
+            }
+            walk_pair(ra, rb, ca, cb, real_b, T.nstart, T.nend, o);
+            if (T.flags & SERVE_FINAL) {
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    if (h == 1 && !real_b) break;
+                    const Prime& c = h ? cb : ca;
+                    const u64 s7 = to_mont(T.nend, c);
+                    u32 back = (u32)mont_mul(s7, 1, c.p, c.pinv);
+                    if (c.p <= T.nend && T.nend % c.p == back) back = T.nend;
+                    bad += back != T.nend;
+                    sum += (h ? rb : ra) + s7;
+                }
+            } else {
+                T.residue[ia] = ra;
+                if (real_b) T.residue[ib] = rb;
+            }
+        }
+        if (T.flags & SERVE_FINAL) {
+#pragma unroll
+            for (int d = 16; d; d >>= 1) {
+                sum += __shfl_xor_sync(0xffffffffu, sum, d);
+                bad += __shfl_xor_sync(0xffffffffu, bad, d);
+            }
+            if ((threadIdx.x & 31) == 0) {
+                wsum[threadIdx.x >> 5] = sum;
+                wbad[threadIdx.x >> 5] = bad;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                u64 s = 0;
+                u32 b = 0;
+                for (int w = 0; w < (int)(blockDim.x / 32); ++w) {
+                    s += wsum[w];
+                    b += wbad[w];
+                }
+                if (s) atomicAdd(&T.ctr->raw_sum, s);
+                if (b) atomicOr(&T.ctr->flags, FLAG_VALIDATION);
+            }
+        }
+    }
+    __syncthreads();
+    const u32 nh = st.n < kHitStage ? st.n : kHitStage;
+    if (nh) {
+        __shared__ u32 gbase;
+        if (threadIdx.x == 0) gbase = atomicAdd(&a.gctr->nhits, nh);
+        __syncthreads();
+        for (u32 k = threadIdx.x; k < nh; k += blockDim.x) {
+            const u32 g = gbase + k;
+            if (g < a.hitcap)
+                a.hits[g] = st.buf[k];
+            else
+                atomicOr(&a.gctr->flags, FLAG_HIT_OVERFLOW);
+        }
+    }
+}
+
 // ========================================================== table check ====
 
 // Direct product 2*3*...*n0 mod the first candidate, reduced over the grid
@@ -742,6 +848,15 @@ cudaError_t batch_occupancy(int* blocks_per_sm) {
 }
 
 int batch_max_jobs() { return kBatchMaxJobs; }
+
+cudaError_t launch_serve_round(const ServeArgs& a, int grid, cudaStream_t s) {
+    serve_round_kernel<<<grid, kSieveThreads, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t serve_occupancy(int* blocks_per_sm) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, serve_round_kernel, kSieveThreads, 0);
+}
 
 cudaError_t launch_table_check(const TableCheckArgs& a, int grid, cudaStream_t s) {
     table_check_kernel<<<grid, 256, 0, s>>>(a);

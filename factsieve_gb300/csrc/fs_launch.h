@@ -80,6 +80,38 @@ struct BatchArgs {
     u32 hitcap;
 };
 
+// Serving round: one chunk = a block of one job's candidates in one phase;
+// the kernel cuts chunks into tiles of 2 x 256 candidates.
+enum : u32 { SERVE_SETUP = 1u, SERVE_FINAL = 2u };
+struct ServeChunk {
+    const u64* cand;
+    u64* residue;
+    Counters* ctr;               // the job's counters (raw_sum, flags)
+    const u64* words;            // the job's setup plan
+    const Layer* layers;
+    u64 deficit;
+    u32 layer_begin, layer_end;
+    u32 first, count;            // candidates [first, first + count)
+    u32 nstart, nend;            // walk [nstart, nend); final: s7 = nend * R
+    u32 flags;                   // SERVE_SETUP: start from the plan; SERVE_FINAL: checksum, no store
+    u32 tag;                     // job slot, stored in hit records
+    u32 tile_end;                // inclusive prefix of tiles over the round's chunks
+    u32 pad;
+};
+
+constexpr int kServeMaxChunks = 4096;
+
+struct ServeArgs {
+    const ServeChunk* chunks;
+    u32 nchunks;
+    u32* tile_counter;
+    Counters* gctr;              // round-wide hit count and overflow flag
+    Factor* hits;
+    u32 hitcap;
+};
+
+cudaError_t launch_serve_round(const ServeArgs& a, int grid, cudaStream_t s);
+cudaError_t serve_occupancy(int* blocks_per_sm);
 cudaError_t launch_gen(const GenArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_batch(const BatchArgs& a, int grid, cudaStream_t s);
 cudaError_t batch_occupancy(int* blocks_per_sm);

@@ -144,6 +144,46 @@ int fs_batch_collect(fs_ctx *ctx, fs_job_result *results, fs_factor *hits, uint6
 /* Free the batch's device memory and graph. */
 int fs_batch_release(fs_ctx *ctx);
 
+/* ---- serving: continuous batching of search requests ----------------------- */
+/* No counterpart in the reference.  Requests queue on the host; each
+ * fs_serve_round() admits queued jobs while a slot is free and the device
+ * keeps mem_reserve bytes free (cudaMemGetInfo), gives every working job an
+ * equal share of round_budget -- starting residues for its next candidates or
+ * the next chunk of its n-walk over all of them, residues staying in its
+ * device buffer between rounds -- runs all of it as one persistent launch,
+ * waits, and retires finished jobs.  A job's result equals a search of that
+ * job alone. */
+typedef struct {
+    uint32_t max_active;     /* jobs resident on the device at once (<= 4096) */
+    uint32_t hitcap;         /* hit records one round can hold */
+    uint64_t round_budget;   /* (p,n) steps of work per round; 0: 3e10 (about 20 ms) */
+    uint64_t mem_reserve;    /* device bytes admission leaves free */
+} fs_serve_config;
+
+typedef struct {
+    int64_t id;              /* as given to fs_serve_submit */
+    uint64_t raw_sum;        /* sum of (s6 + s7) over the job's candidates */
+    uint64_t primecount;     /* candidates */
+    uint64_t nhits;          /* hits (before the 2-PRP filter), at hits[hit_offset...] */
+    uint32_t flags;          /* FS_FLAG_* */
+    uint32_t pad;
+    double t_submit, t_admit, t_done;   /* fs_clock() seconds */
+    uint64_t hit_offset;
+} fs_served;
+
+double fs_clock(void);       /* steady clock, seconds */
+int fs_serve_create(fs_ctx *ctx, const fs_serve_config *cfg);
+int fs_serve_submit(fs_ctx *ctx, const fs_job *job, int64_t id);
+/* One round (blocks until its GPU work is done); reports jobs on the device
+ * and jobs still queued. */
+int fs_serve_round(fs_ctx *ctx, uint32_t *n_active, uint32_t *n_queued);
+/* Pop up to cap finished jobs, copying their hits into hits[0..hitcap). */
+int fs_serve_poll(fs_ctx *ctx, fs_served *out, uint32_t cap, uint32_t *n, fs_factor *hits, uint64_t hitcap,
+                  uint64_t *nhits);
+/* Rounds run and (p,n) walk steps served so far. */
+int fs_serve_stats(fs_ctx *ctx, uint64_t *rounds, uint64_t *served_steps);
+int fs_serve_destroy(fs_ctx *ctx);
+
 /* ---- stage-level kernels on caller device buffers ------------------------ */
 /* getsegprimes (getsegprimes.cl:170-239): append the candidates of
  * [low, high) to d_cand at slot d_ctr->ncand (the reference's

@@ -1,0 +1,54 @@
+"""The serving loop: jobs admitted while others are resident, advanced in
+shared rounds with residues kept on the device, each finish with the same
+bits as the job searched alone."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+from test_gpu_batch import JOBS
+
+
+def test_served_jobs_equal_each_job_alone(ctx):
+    import factsieve_gb300 as fs
+    from factsieve_gb300.serve import Server
+    alone = {k: ctx.sieve(*j, threads=8) for k, j in enumerate(JOBS)}
+    # a small round budget forces many rounds: setup split over candidates,
+    # walks split into chunks, jobs joining while others are mid-walk
+    srv = Server(ctx, max_active=3, round_budget=2_000_000_000, mem_reserve=1 << 30)
+    done = {}
+    pending = list(enumerate(JOBS))
+    rounds = 0
+    try:
+        while len(done) < len(JOBS):
+            if pending and rounds % 2 == 0:
+                k, j = pending.pop(0)
+                srv.submit(j, k)
+            srv.round()
+            rounds += 1
+            for d in srv.poll():
+                done[d["id"]] = d
+            assert rounds < 5000
+    finally:
+        srv.close()
+    assert rounds > len(JOBS)
+    for k, d in done.items():
+        a = alone[k]
+        kept, cs_add, disc = fs.postprocess(d["hits"], threads=8)
+        assert d["flags"] == 0, JOBS[k]
+        assert (d["primecount"], d["raw_sum"], len(d["hits"])) == (a.primecount, a.raw_sum, a.nhits), JOBS[k]
+        assert (d["raw_sum"] + cs_add) & ((1 << 64) - 1) == a.checksum
+        assert kept[["p", "nc"]].tolist() == a.factors[["p", "nc"]].tolist()
+        assert d["t_submit"] <= d["t_admit"] <= d["t_done"]
+
+
+def test_admission_waits_for_device_memory(ctx):
+    from factsieve_gb300.serve import Server
+    srv = Server(ctx, max_active=4, mem_reserve=1 << 60)   # more than any GPU has
+    try:
+        srv.submit(JOBS[0], 7)
+        active, queued = srv.round()
+        assert (active, queued) == (0, 1)
+        assert srv.poll() == []
+    finally:
+        srv.close()
