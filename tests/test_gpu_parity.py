@@ -199,6 +199,10 @@ def test_hit_overflow_is_reported(ctx):
     ((1 << 63) + 1, (1 << 63) + 300_000, 5_000, 5_700),             # canonical 96-bit step (p >= 2^63)
     ((1 << 64) - 400_000, (1 << 64) - 1, 1_000, 1_333),              # canonical 96-bit step near 2^64
     (4 * 10**12, 4 * 10**12 + 200_000, 1_000_000, 1_000_300),      # across the 64/96-bit boundary
+    (10**12, 10**12 + 300_000, 100_000, 100_700),                  # lazy 64-bit step
+    ((1 << 36) + 1, (1 << 36) + 300_000, 500_000, 500_300),        # lazy 64-bit step, large multipliers
+    ((1 << 33) - 150_000, (1 << 33) + 150_000, 2000, 2900),         # generic / lazy boundary at 2^33
+    (8 * 10**12, 8 * 10**12 + 300_000, 524_000, 524_400),          # multipliers across 2^19
 ])
 def test_walk_regimes_match_oracle(ctx, orc, lo, hi, nmin, nmax):
     """Every walk regime (and a pair straddling two) gives the oracle's residues, sums and hits."""
@@ -243,7 +247,7 @@ def test_walk_with_multipliers_beyond_2p28(ctx, orc):
     assert int(c["flags"]) == 0
 
 
-@pytest.mark.parametrize("name", ["config3_slice100", "config2_slice100", "selftest1"])
+@pytest.mark.parametrize("name", ["config3_slice100", "config2_slice100", "selftest1", "config3", "config2"])
 def test_search_matches_long_fixture(ctx, name):
     g = _golden(name)
     r = ctx.sieve(g["pmin"], g["pmax"], g["nmin"], g["nmax"], threads=16)
