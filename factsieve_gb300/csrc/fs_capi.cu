@@ -252,7 +252,7 @@ int run_table_check(fs_ctx* c, const u64* d_cand, fs::Counters* d_ctr, uint32_t 
 // threads when auto_chunks() says so.
 int run_sieve(fs_ctx* c, const u64* d_cand, uint32_t cap, fs::Counters* d_ctr, uint32_t nstart,
               uint32_t nend, uint32_t nmax, bool count, uint64_t est_cand, fs::Factor* d_hits,
-              uint32_t hitcap) {
+              uint32_t hitcap, uint64_t plo, uint64_t phi) {
     uint32_t chunks = auto_chunks(c, est_cand, nstart);
     PlanGPU* pl = nullptr;
     int rc = get_plan(c, nstart, chunks, &pl);
@@ -289,6 +289,7 @@ int run_sieve(fs_ctx* c, const u64* d_cand, uint32_t cap, fs::Counters* d_ctr, u
     bool first = true;
     do {
         uint32_t e = split ? std::min<uint64_t>((uint64_t)s + maxs, nend) : nend;
+        const int walk = fs::walk_for_range(plo, phi, e);
         const bool fin = (e == nend);
         a.nstart = s;
         a.nend = e;
@@ -297,7 +298,7 @@ int run_sieve(fs_ctx* c, const u64* d_cand, uint32_t cap, fs::Counters* d_ctr, u
         a.store_final = 0;
         std::pair<cudaEvent_t, cudaEvent_t> ev;
         if ((rc = ev_begin(c, &ev))) return rc;
-        CK(c, fs::launch_sieve(a, first ? setup_mode : fs::SETUP_LOAD, fin, grid, c->stream, variant(c)));
+        CK(c, fs::launch_sieve(a, first ? setup_mode : fs::SETUP_LOAD, fin, grid, c->stream, variant(c), walk));
         if ((rc = ev_end(c, ev, c->sieve_ev))) return rc;
         ++c->launches;
         ++c->sieve_launches;
@@ -546,7 +547,7 @@ int fs_search_segment(fs_ctx* c, uint64_t low, uint64_t high) {
         c->table_checked = true;
     }
     return run_sieve(c, c->d_cand, cap, c->d_ctr, c->nmin, c->nmax, c->nmax, true,
-                     est_candidates(low, high), c->d_hits, c->hit_cap);
+                     est_candidates(low, high), c->d_hits, c->hit_cap, low, high);
 }
 
 int fs_search_range(fs_ctx* c, uint64_t low, uint64_t high, uint64_t seg_width) {
@@ -622,7 +623,7 @@ int fs_setup(fs_ctx* c, const uint64_t* d_cand, uint32_t cap, fs_counters* d_ctr
         CK(c, fs::launch_setup_partial(a, std::max(1, sieve_grid(c) / (int)chunks), (int)chunks, c->stream));
         mode = fs::SETUP_PARTIALS;
     }
-    CK(c, fs::launch_sieve(a, mode, false, sieve_grid(c), c->stream, variant(c)));
+    CK(c, fs::launch_sieve(a, mode, false, sieve_grid(c), c->stream, variant(c), fs::WALK_ANY));
     return FS_OK;
 }
 
@@ -646,7 +647,7 @@ int fs_iterate(fs_ctx* c, const uint64_t* d_cand, uint32_t cap, fs_counters* d_c
         uint32_t e = (maxs && nend - s > maxs) ? s + maxs : nend;
         a.nstart = s;
         a.nend = e;
-        CK(c, fs::launch_sieve(a, fs::SETUP_LOAD, false, sieve_grid(c), c->stream, variant(c)));
+        CK(c, fs::launch_sieve(a, fs::SETUP_LOAD, false, sieve_grid(c), c->stream, variant(c), fs::WALK_ANY));
         s = e;
     } while (s < nend);
     return FS_OK;
@@ -667,7 +668,7 @@ int fs_check(fs_ctx* c, const uint64_t* d_cand, uint32_t cap, fs_counters* d_ctr
     a.nmax = nmax;
     a.count_candidates = 1;
     a.store_final = 0;
-    CK(c, fs::launch_sieve(a, fs::SETUP_LOAD, true, sieve_grid(c), c->stream, variant(c)));
+    CK(c, fs::launch_sieve(a, fs::SETUP_LOAD, true, sieve_grid(c), c->stream, variant(c), fs::WALK_ANY));
     return FS_OK;
 }
 

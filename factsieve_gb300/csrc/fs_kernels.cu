@@ -334,6 +334,13 @@ __device__ __forceinline__ void walk_one(u64& r, const Prime& c, int reg, u32 ns
     }
 }
 
+// Walk both candidates of a pair with one step the host has shown valid for
+// every candidate of the launch (WALK_T64 / WALK_L96 / WALK_C96), or, for
+// WALK_ANY, each with the fastest step that applies to it.
+template <int WALK>
+__device__ __forceinline__ void walk_pair_as(u64& ra, u64& rb, const Prime& a, const Prime& b, bool real_b,
+                                             u32 nstart, u32 nend, const WalkOut& o);
+
 // Walk both candidates of a pair, each with the fastest step that applies.
 __device__ __forceinline__ void walk_pair(u64& ra, u64& rb, const Prime& a, const Prime& b, bool real_b,
                                           u32 nstart, u32 nend, const WalkOut& o) {
@@ -349,6 +356,16 @@ __device__ __forceinline__ void walk_pair(u64& ra, u64& rb, const Prime& a, cons
     }
     walk_one(ra, a, ga, nstart, nend, o);
     if (real_b) walk_one(rb, b, gb, nstart, nend, o);
+}
+
+template <int WALK>
+__device__ __forceinline__ void walk_pair_as(u64& ra, u64& rb, const Prime& a, const Prime& b, bool real_b,
+                                             u32 nstart, u32 nend, const WalkOut& o) {
+    if (nstart >= nend) return;
+    if (WALK == WALK_T64) walk_reg_pair<RegT64>(ra, rb, a, b, real_b, nstart, nend, o);
+    else if (WALK == WALK_L96) walk_reg_pair<RegL96>(ra, rb, a, b, real_b, nstart, nend, o);
+    else if (WALK == WALK_C96) walk_reg_pair<RegC96>(ra, rb, a, b, real_b, nstart, nend, o);
+    else walk_pair(ra, rb, a, b, real_b, nstart, nend, o);
 }
 
 // Starting residue of candidate i (SETUP mode), before the walk.
@@ -368,7 +385,7 @@ __device__ __forceinline__ u64 start_residue_one(const SieveArgs& a, const Prime
     return r;
 }
 
-template <int SETUP, bool FINAL, int MINB>
+template <int SETUP, bool FINAL, int MINB, int WALK>
 __global__ void __launch_bounds__(kSieveThreads, MINB) sieve_kernel(SieveArgs a) {
     __shared__ HitStage st;
     __shared__ u64 wsum[kSieveThreads / 32];
@@ -396,7 +413,7 @@ __global__ void __launch_bounds__(kSieveThreads, MINB) sieve_kernel(SieveArgs a)
             ra = start_residue_one<SETUP>(a, ca, ia);
             rb = real_b ? start_residue_one<SETUP>(a, cb, ib) : ra;
         }
-        walk_pair(ra, rb, ca, cb, real_b, a.nstart, a.nend, o);
+        walk_pair_as<WALK>(ra, rb, ca, cb, real_b, a.nstart, a.nend, o);
         if (FINAL) {
             // s7 = nmax*R mod p, the reference's final Montgomery image of n
 #pragma unroll
@@ -804,29 +821,38 @@ cudaError_t launch_gen(const GenArgs& a, int grid, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-template <int MINB>
-static void launch_sieve_v(const SieveArgs& a, int setup, bool fin, int grid, cudaStream_t s) {
+template <int MINB, int WALK>
+static void launch_sieve_w(const SieveArgs& a, int setup, bool fin, int grid, cudaStream_t s) {
     const int t = kSieveThreads;
     if (setup == SETUP_PLAN) {
-        if (fin) sieve_kernel<SETUP_PLAN, true, MINB><<<grid, t, 0, s>>>(a);
-        else sieve_kernel<SETUP_PLAN, false, MINB><<<grid, t, 0, s>>>(a);
+        if (fin) sieve_kernel<SETUP_PLAN, true, MINB, WALK><<<grid, t, 0, s>>>(a);
+        else sieve_kernel<SETUP_PLAN, false, MINB, WALK><<<grid, t, 0, s>>>(a);
     } else if (setup == SETUP_PARTIALS) {
-        if (fin) sieve_kernel<SETUP_PARTIALS, true, MINB><<<grid, t, 0, s>>>(a);
-        else sieve_kernel<SETUP_PARTIALS, false, MINB><<<grid, t, 0, s>>>(a);
+        if (fin) sieve_kernel<SETUP_PARTIALS, true, MINB, WALK><<<grid, t, 0, s>>>(a);
+        else sieve_kernel<SETUP_PARTIALS, false, MINB, WALK><<<grid, t, 0, s>>>(a);
     } else {
-        if (fin) sieve_kernel<SETUP_LOAD, true, MINB><<<grid, t, 0, s>>>(a);
-        else sieve_kernel<SETUP_LOAD, false, MINB><<<grid, t, 0, s>>>(a);
+        if (fin) sieve_kernel<SETUP_LOAD, true, MINB, WALK><<<grid, t, 0, s>>>(a);
+        else sieve_kernel<SETUP_LOAD, false, MINB, WALK><<<grid, t, 0, s>>>(a);
     }
 }
 
 // variant v: the kernel compiled for v resident blocks per SM (register cap
-// 65536 / (256 v)); 0 picks the default.
+// 65536 / (256 v)); 0 picks the default.  walk: a step valid for every
+// candidate of the launch (WALK_ANY: chosen per candidate).  The specialised
+// walks are built for the default variant only.
 cudaError_t launch_sieve(const SieveArgs& a, int setup, bool final_chunk, int grid, cudaStream_t s,
-                         int variant) {
-    switch (variant) {
-        case 2: launch_sieve_v<2>(a, setup, final_chunk, grid, s); break;
-        case 4: launch_sieve_v<4>(a, setup, final_chunk, grid, s); break;
-        default: launch_sieve_v<3>(a, setup, final_chunk, grid, s); break;
+                         int variant, int walk) {
+    if (variant == 2) {
+        launch_sieve_w<2, WALK_ANY>(a, setup, final_chunk, grid, s);
+    } else if (variant == 4) {
+        launch_sieve_w<4, WALK_ANY>(a, setup, final_chunk, grid, s);
+    } else {
+        switch (walk) {
+            case WALK_T64: launch_sieve_w<3, WALK_T64>(a, setup, final_chunk, grid, s); break;
+            case WALK_L96: launch_sieve_w<3, WALK_L96>(a, setup, final_chunk, grid, s); break;
+            case WALK_C96: launch_sieve_w<3, WALK_C96>(a, setup, final_chunk, grid, s); break;
+            default: launch_sieve_w<3, WALK_ANY>(a, setup, final_chunk, grid, s); break;
+        }
     }
     return cudaGetLastError();
 }
@@ -868,16 +894,27 @@ cudaError_t launch_imad_bench(u32 iters, u32 kind, u32 seed, u32* sink, int grid
     return cudaGetLastError();
 }
 
+int walk_for_range(uint64_t plo, uint64_t phi, uint32_t kmax) {
+    if (phi <= plo || kmax == 0) return WALK_ANY;
+    const uint64_t pmax = phi - 1;
+    const int kb = 32 - __builtin_clz(kmax);
+    // the lazy 64-bit step needs p > 2^33 and p kmax <= 2^62 (lazy_ok)
+    if (plo > (1ull << 33) && pmax <= ((1ull << 62) / kmax)) return WALK_T64;
+    if (kb <= 28 && plo > (1ull << 33) && (pmax >> 63) == 0) return WALK_L96;
+    if (kb <= 28 && (plo >> 63) != 0) return WALK_C96;
+    return WALK_ANY;
+}
+
 int sieve_threads() { return kSieveThreads; }
 int gen_threads() { return kGenWarps * 32; }
 
 cudaError_t sieve_occupancy(int* blocks_per_sm, int variant) {
     switch (variant) {
-        case 2: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, sieve_kernel<SETUP_PLAN, true, 2>,
+        case 2: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, sieve_kernel<SETUP_PLAN, true, 2, WALK_ANY>,
                                                                      kSieveThreads, 0);
-        case 4: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, sieve_kernel<SETUP_PLAN, true, 4>,
+        case 4: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, sieve_kernel<SETUP_PLAN, true, 4, WALK_ANY>,
                                                                      kSieveThreads, 0);
-        default: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, sieve_kernel<SETUP_PLAN, true, 3>,
+        default: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, sieve_kernel<SETUP_PLAN, true, 3, WALK_ANY>,
                                                                       kSieveThreads, 0);
     }
 }

@@ -8,6 +8,8 @@
 namespace fs {
 
 enum { SETUP_LOAD = 0, SETUP_PLAN = 1, SETUP_PARTIALS = 2 };
+// Walk step used for every candidate of a launch (WALK_ANY: per candidate).
+enum { WALK_ANY = 0, WALK_T64 = 1, WALK_L96 = 2, WALK_C96 = 3 };
 
 // Candidate generator over the odd numbers o0 + 2 j < high.
 struct GenArgs {
@@ -116,7 +118,10 @@ cudaError_t launch_gen(const GenArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_batch(const BatchArgs& a, int grid, cudaStream_t s);
 cudaError_t batch_occupancy(int* blocks_per_sm);
 int batch_max_jobs();
-cudaError_t launch_sieve(const SieveArgs& a, int setup, bool final_chunk, int grid, cudaStream_t s, int variant);
+cudaError_t launch_sieve(const SieveArgs& a, int setup, bool final_chunk, int grid, cudaStream_t s, int variant,
+                         int walk);
+// The walk step valid for every p in [plo, phi) with multipliers up to kmax.
+int walk_for_range(uint64_t plo, uint64_t phi, uint32_t kmax);
 cudaError_t launch_setup_partial(const SieveArgs& a, int grid_x, int nchunks, cudaStream_t s);
 cudaError_t launch_table_check(const TableCheckArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_imad_bench(u32 iters, u32 kind, u32 seed, u32* sink, int grid, cudaStream_t s);

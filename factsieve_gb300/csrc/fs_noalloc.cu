@@ -108,7 +108,8 @@ extern "C" int fs_segment_noalloc(uint64_t low, uint64_t high, uint32_t nmin, ui
     a.hits = (fs::Factor*)d_hits;
     a.hitcap = hitcap;
     a.ctr = ctr;
-    if (fs::launch_sieve(a, fs::SETUP_PLAN, true, ds->sm_count * ds->blocks_per_sm, s, 3) != cudaSuccess)
+    if (fs::launch_sieve(a, fs::SETUP_PLAN, true, ds->sm_count * ds->blocks_per_sm, s, 3, fs::WALK_ANY) !=
+        cudaSuccess)
         return FS_E_CUDA;
     return FS_OK;
 }
