@@ -50,6 +50,13 @@ WORKLOADS = {
     "config3": (1 << 63, (1 << 63) + 1_000_000_000, 1_000_000, 1_010_000, 100_000_000),
 }
 IMAD_PER_PRODUCT = 20   # reference m_mul on 32-bit limbs (8 mul_wide + 4 + 8)
+# DRAM bytes (read + write) per sieve launch and IMAD-pipe busy share from
+# one ncu --set full capture of one launch of the same workload
+# (profiles/sieve_kernel_config2.md, profiles/sieve_kernel_config3.md)
+NCU_CAPTURE = {
+    "config2": {"traffic": 29_146_880, "imad_pipe_busy": 0.811, "source": "profiles/sieve_kernel_config2.md"},
+    "config3": {"traffic": 18_760_960, "imad_pipe_busy": 0.861, "source": "profiles/sieve_kernel_config3.md"},
+}
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 
 
@@ -274,8 +281,11 @@ def run_ours(args):
     achieved = products / sieve_s / 1e9 if sieve_s > 0 else 0.0
     imad_ops, _ = ctx.bench_int_pipe(0, 20000)
     peak = imad_ops / IMAD_PER_PRODUCT / 1e9
+    cap = NCU_CAPTURE.get(wl, {})
     roof = {"bound": "imad", "achieved": achieved, "peak": peak, "unit": "Gmulmod/s",
-            "frac": achieved / peak if peak else None, "traffic": None,
+            "frac": achieved / peak if peak else None, "traffic": cap.get("traffic"),
+            "imad_pipe_busy_ncu": cap.get("imad_pipe_busy"), "ncu_source": cap.get("source"),
+            "algorithmic_bytes_per_launch": 8 * my_pc / max(st["sieve_launches"], 1),
             "kernel": "sieve_kernel (setup+iterate+check, fused)",
             "kernel_ms_per_launch": st["sieve_ms"] / max(st["sieve_launches"], 1),
             "products_per_launch": products / max(st["sieve_launches"], 1),
