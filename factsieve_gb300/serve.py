@@ -52,7 +52,7 @@ def _declare():
     L.fs_serve_poll.argtypes = [vp, C.POINTER(Served), u32, C.POINTER(u32), C.POINTER(Factor), u64,
                                 C.POINTER(u64)]
     L.fs_serve_stats.restype = C.c_int
-    L.fs_serve_stats.argtypes = [vp, C.POINTER(u64), C.POINTER(u64)]
+    L.fs_serve_stats.argtypes = [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.fs_serve_destroy.restype = C.c_int
     L.fs_serve_destroy.argtypes = [vp]
     _declared = True
@@ -107,8 +107,9 @@ class Server:
 
     def stats(self):
         r, s = C.c_uint64(0), C.c_uint64(0)
-        lib().fs_serve_stats(self.ctx.handle, C.byref(r), C.byref(s))
-        return {"rounds": r.value, "served_pair_steps": s.value}
+        su, km = C.c_double(0), C.c_double(0)
+        lib().fs_serve_stats(self.ctx.handle, C.byref(r), C.byref(s), C.byref(su), C.byref(km))
+        return {"rounds": r.value, "served_pair_steps": s.value, "setup_units": su.value, "kernel_ms": km.value}
 
     def close(self):
         if self.ctx is not None:
@@ -164,6 +165,9 @@ def run_stream(ctx, requests, stop_after_s, max_active=64, round_budget=0, mem_r
         "unfinished": submitted - len(done), "elapsed_s": elapsed, "rounds": st["rounds"],
         "served_pair_steps": st["served_pair_steps"],
         "served_pair_steps_per_s": st["served_pair_steps"] / elapsed if elapsed > 0 else 0.0,
+        "gpu_busy_fraction": st["kernel_ms"] * 1e-3 / elapsed if elapsed > 0 else 0.0,
+        "setup_share_of_work": (st["setup_units"] / (st["setup_units"] + st["served_pair_steps"])
+                                if st["setup_units"] + st["served_pair_steps"] else 0.0),
         "p50_s": _pct(lat, 50), "p99_s": _pct(lat, 99), "mean_s": float(np.mean(lat)) if lat else None,
     }
     if pair_steps_of is not None:

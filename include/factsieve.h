@@ -180,8 +180,10 @@ int fs_serve_round(fs_ctx *ctx, uint32_t *n_active, uint32_t *n_queued);
 /* Pop up to cap finished jobs, copying their hits into hits[0..hitcap). */
 int fs_serve_poll(fs_ctx *ctx, fs_served *out, uint32_t cap, uint32_t *n, fs_factor *hits, uint64_t hitcap,
                   uint64_t *nhits);
-/* Rounds run and (p,n) walk steps served so far. */
-int fs_serve_stats(fs_ctx *ctx, uint64_t *rounds, uint64_t *served_steps);
+/* Rounds run, (p,n) walk steps served, setup work queued (in walk-step
+ * units: 2.7 per Montgomery product) and CUDA-event time of the drained
+ * round kernels, so far. */
+int fs_serve_stats(fs_ctx *ctx, uint64_t *rounds, uint64_t *served_steps, double *setup_units, double *kernel_ms);
 int fs_serve_destroy(fs_ctx *ctx);
 
 /* ---- stage-level kernels on caller device buffers ------------------------ */
