@@ -27,7 +27,7 @@ LIB_PATH = os.path.join(_HERE, "libfactsieve.so")
 CLI_PATH = os.path.join(_HERE, "bin", "factsieve")
 
 FS_OK, FS_E_ARG, FS_E_CUDA, FS_E_OVERFLOW, FS_E_VALIDATION = 0, 1, 2, 3, 4
-FS_E_TABLE, FS_E_NOMEM, FS_E_VERIFY, FS_E_STATE, FS_E_TIMEOUT = 5, 6, 7, 8, 9
+FS_E_TABLE, FS_E_NOMEM, FS_E_VERIFY, FS_E_STATE, FS_E_LIMIT = 5, 6, 7, 8, 10
 FLAG_VALIDATION, FLAG_CAND_OVERFLOW, FLAG_HIT_OVERFLOW, FLAG_TABLE = 1, 2, 4, 8
 
 FACTOR_DTYPE = np.dtype([("p", "<u8"), ("nc", "<i4"), ("pad", "<i4")])
@@ -100,6 +100,7 @@ def _declare(L):
         "fs_iterate": (C.c_int, [vp, vp, u32, vp, vp, u32, u32, vp, u32]),
         "fs_check": (C.c_int, [vp, vp, u32, vp, vp, u32]),
         "fs_table_check": (C.c_int, [vp, vp, vp, u32, P64]),
+        "fs_plan_check": (C.c_int, [vp, vp, vp, u32, vp, vp, u32, u64, P64]),
         "fs_bench_int_pipe": (C.c_int, [vp, u32, u32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
         "fs_set_timing": (C.c_int, [vp, C.c_int]),
         "fs_get_stats": (C.c_int, [vp, C.POINTER(Stats)]),
@@ -404,6 +405,12 @@ class Context:
             out.append(SieveResult(kept, (r["raw_sum"] + cs_add) & 0xFFFFFFFFFFFFFFFF, r["primecount"], len(kept),
                                    r["raw_sum"], len(mine), disc))
         return out
+
+    def plan_check(self, d_cand, d_ctr, nmin, d_words, d_layers4, nlayers, deficit):
+        out = np.zeros(2, np.uint64)
+        self._chk(lib().fs_plan_check(self._h, C.c_void_p(d_cand), C.c_void_p(d_ctr), nmin, C.c_void_p(d_words),
+                                      C.c_void_p(d_layers4), nlayers, deficit, _p64(out)), "fs_plan_check")
+        return int(out[0]), int(out[1])
 
     # the reference's whole search
     def sieve(self, pmin, pmax, nmin, nmax, threads=2, seg_width=0, result_cap=0) -> SieveResult:

@@ -218,24 +218,35 @@ namespace {
 
 using fs_internal::run_gen;
 
-int run_table_check(fs_ctx* c, const u64* d_cand, fs::Counters* d_ctr, uint32_t n, PlanGPU* pl) {
+// Per-block partial products, the completion counter and the result of the
+// table check, allocated on first use.
+int ensure_check_buffers(fs_ctx* c) {
     if (!c->d_chk_scratch) {
         c->chk_grid = c->sm_count * 4;
         CK(c, cudaMalloc((void**)&c->d_chk_scratch, c->chk_grid * sizeof(u64)));
         CK(c, cudaMalloc((void**)&c->d_chk_done, sizeof(u32)));
         CK(c, cudaMalloc((void**)&c->d_chk_result, 2 * sizeof(u64)));
+        CK(c, cudaMalloc((void**)&c->d_chk_chunk, sizeof(fs::PlanChunkDev)));
         CK(c, cudaMemsetAsync(c->d_chk_done, 0, sizeof(u32), c->stream));
     }
+    return FS_OK;
+}
+
+int run_table_check_raw(fs_ctx* c, const u64* d_cand, fs::Counters* d_ctr, uint32_t n, const u64* words,
+                        const fs::Layer* layers, const fs::PlanChunkDev* chunks, uint32_t nchunks,
+                        uint64_t deficit) {
+    int rc = ensure_check_buffers(c);
+    if (rc) return rc;
     fs::TableCheckArgs t;
     memset(&t, 0, sizeof(t));
     t.cand = d_cand;
     t.ncand = &d_ctr->ncand;
     t.n0 = n;
-    t.words = pl->d_words;
-    t.layers = pl->d_layers;
-    t.chunks = pl->d_chunks;
-    t.nchunks = pl->nchunks;
-    t.deficit = pl->deficit;
+    t.words = words;
+    t.layers = layers;
+    t.chunks = chunks;
+    t.nchunks = nchunks;
+    t.deficit = deficit;
     t.scratch = c->d_chk_scratch;
     t.done = c->d_chk_done;
     t.result = c->d_chk_result;
@@ -244,6 +255,11 @@ int run_table_check(fs_ctx* c, const u64* d_cand, fs::Counters* d_ctr, uint32_t 
     CK(c, fs::launch_table_check(t, c->chk_grid, c->stream));
     ++c->launches;
     return FS_OK;
+}
+
+int run_table_check(fs_ctx* c, const u64* d_cand, fs::Counters* d_ctr, uint32_t n, PlanGPU* pl) {
+    return run_table_check_raw(c, d_cand, d_ctr, n, pl->d_words, pl->d_layers, pl->d_chunks, pl->nchunks,
+                               pl->deficit);
 }
 
 // setup + iterate + check of the candidates in d_cand over [nstart, nend),
@@ -334,7 +350,6 @@ const char* fs_strerror(int code) {
         case FS_E_NOMEM: return "out of memory";
         case FS_E_VERIFY: return "CPU factor verification failed";
         case FS_E_STATE: return "call out of order";
-        case FS_E_TIMEOUT: return "timed out";
         case FS_E_LIMIT: return "request exceeds a fixed size limit";
         default: return "unknown error";
     }
@@ -404,6 +419,7 @@ int fs_destroy(fs_ctx* c) {
     cudaFree(c->d_chk_scratch);
     cudaFree(c->d_chk_done);
     cudaFree(c->d_chk_result);
+    cudaFree(c->d_chk_chunk);
     cudaFree(c->d_sink);
     fs_batch_release(c);
     fs_serve_destroy(c);
@@ -684,6 +700,23 @@ int fs_table_check(fs_ctx* c, const uint64_t* d_cand, fs_counters* d_ctr, uint32
         CK(c, cudaMemcpyAsync(out2, c->d_chk_result, 2 * sizeof(u64), cudaMemcpyDeviceToHost, c->stream));
         CK(c, cudaStreamSynchronize(c->stream));
     }
+    return FS_OK;
+}
+
+int fs_plan_check(fs_ctx* c, const uint64_t* d_cand, fs_counters* d_ctr, uint32_t nmin, const uint64_t* d_words,
+                  const uint32_t* d_layers4, uint32_t nlayers, uint64_t deficit, uint64_t* out2) {
+    if (!c || !d_cand || !d_ctr || (nlayers && (!d_words || !d_layers4))) return FS_E_ARG;
+    int rc = bind(c);
+    if (rc || (rc = ensure_check_buffers(c))) return rc;
+    const fs::PlanChunkDev one{0, nlayers, deficit};
+    CK(c, cudaMemcpyAsync(c->d_chk_chunk, &one, sizeof(one), cudaMemcpyHostToDevice, c->stream));
+    if ((rc = run_table_check_raw(c, (const u64*)d_cand, (fs::Counters*)d_ctr, nmin, (const u64*)d_words,
+                                  (const fs::Layer*)d_layers4, c->d_chk_chunk, 1, deficit)))
+        return rc;
+    if (out2) {
+        CK(c, cudaMemcpyAsync(out2, c->d_chk_result, 2 * sizeof(u64), cudaMemcpyDeviceToHost, c->stream));
+    }
+    CK(c, cudaStreamSynchronize(c->stream));   // `one` and out2 are host locals
     return FS_OK;
 }
 

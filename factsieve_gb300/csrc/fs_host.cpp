@@ -23,7 +23,7 @@ std::vector<uint32_t> primes_upto(uint32_t n) {
         base.push_back(i);
         for (uint64_t j = (uint64_t)i * i; j <= root; j += 2 * i) small[j] = 1;
     }
-    out.reserve((size_t)(n / (std::log((double)n) - 1.1)) + 16);
+    out.reserve((size_t)(n / std::max(std::log((double)n) - 1.1, 1.0)) + 16);   // pi(n) < n / (ln n - 1.1)
     const uint64_t SEG = 1u << 19;  // odd numbers per segment
     std::vector<uint8_t> seg(SEG);
     for (uint64_t lo = 3; lo <= n; lo += 2 * SEG) {

@@ -52,6 +52,7 @@ struct fs_ctx {
     u64* d_chk_scratch = nullptr;
     u32* d_chk_done = nullptr;
     u64* d_chk_result = nullptr;
+    fs::PlanChunkDev* d_chk_chunk = nullptr;
     int chk_grid = 0;
     u32* d_sink = nullptr;
     std::map<std::pair<uint32_t, uint32_t>, fs_internal::PlanGPU> plans;

@@ -33,7 +33,6 @@ extern "C" {
 #define FS_E_NOMEM 6       /* device or host allocation failed */
 #define FS_E_VERIFY 7      /* a hit failed CPU verification (cl_sieve.cpp:502-506) */
 #define FS_E_STATE 8       /* call out of order (e.g. segment before begin) */
-#define FS_E_TIMEOUT 9     /* a bounded wait gave up */
 #define FS_E_LIMIT 10      /* request larger than a fixed, compiled-in limit */
 
 /* Factor record, layout of the reference's `factor` (cl_sieve.h:3-6):
@@ -212,6 +211,15 @@ int fs_check(fs_ctx *ctx, const uint64_t *d_cand, uint32_t cap, fs_counters *d_c
  * receives {direct, table}. */
 int fs_table_check(fs_ctx *ctx, const uint64_t *d_cand, fs_counters *d_ctr, uint32_t nmin,
                    uint64_t *out2);
+
+/* The same check for a setup plan the caller placed in device memory (as
+ * fs_setup_plan returns it; e.g. the plan handed to fs_segment_noalloc):
+ * FS_FLAG_TABLE is set in d_ctr->flags when it does not multiply to nmin!.
+ * d_words must not be NULL when nlayers > 0, even for a plan with no words
+ * (n <= 2).  No counterpart in the reference, which only checks the table it
+ * built itself (cl_sieve.cpp:903-907). */
+int fs_plan_check(fs_ctx *ctx, const uint64_t *d_cand, fs_counters *d_ctr, uint32_t nmin, const uint64_t *d_words,
+                  const uint32_t *d_layers4, uint32_t nlayers, uint64_t deficit, uint64_t *out2);
 
 /* ---- measurement ---------------------------------------------------------- */
 typedef struct {

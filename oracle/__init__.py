@@ -289,3 +289,41 @@ def postprocess(hits: np.ndarray):
     if k < 0:
         return None
     return arr[:k].copy(), cs.value, disc.value
+
+
+def exact_small(pmin: int, pmax: int, nmin: int, nmax: int) -> dict:
+    """The search by its definition, in pure Python, for small cases at the
+    edge of the domain where the reference's own code does not compute it:
+
+    * nmin in {2, 3}: getPower (cl_sieve.cpp:773-788) leaves curBit at 2^31
+      when the power of 2 in nmin! is 1, so setup.cl:62-72 squares 2 thirty-one
+      more times and the starting residue is not nmin!;
+    * nmin = 1: the power table is empty and setup reads an unset entry 0;
+    * hits with n < 34: the CPU verifier (verifyprime.c:146-173) starts from
+      34! and rejects them, so the reference stops with a verification error.
+
+    Same candidate set (``candidates``); hits are (p, -n) when p | n! - 1 and
+    (p, +n) when p | n! + 1 for n in [nmin, nmax); raw_sum adds nmax! R + nmax R
+    (R = 2^64, residues mod p) per candidate; the checksum adds n + c for each
+    hit whose p is prime (all hits are true, so none is rejected)."""
+    cand = [int(x) for x in candidates(pmin, pmax)]
+    R = 1 << 64
+    M = (1 << 64) - 1
+    hits, raw = [], 0
+    for p in cand:
+        r = 1
+        for k in range(2, nmin + 1):
+            r = r * k % p
+        for n in range(nmin, nmax):
+            if r == 1:
+                hits.append((p, -n))
+            elif r == p - 1:
+                hits.append((p, n))
+            r = r * (n + 1) % p
+        raw += r * R % p + nmax * R % p
+    kept = [(p, nc) for p, nc in sorted(hits, key=lambda h: (h[0], abs(h[1]), h[1])) if is_prime(p)]
+    cs = raw
+    for _, nc in kept:
+        cs += (abs(nc) + (1 if nc > 0 else -1)) & 0xFFFFFFFF
+    return {"primecount": len(cand), "raw_sum": raw & M, "checksum": cs & M, "factorcount": len(kept),
+            "factors": kept, "nhits": len(hits)}

@@ -106,3 +106,17 @@ def test_cli_self_test(fslib, tmp_path):
     assert r.returncode == 0, r.stdout[-3000:]
     assert r.stdout.count("passed.") == 5
     assert "All test cases completed successfully!" in r.stdout
+
+
+def test_cli_top_of_the_p_range(fslib, orc, tmp_path):
+    """-P 18446744073709551615, the largest value the parser accepts: candidates up to 2^64 - 1."""
+    import factsieve_gb300 as fs
+    pmin, pmax, nmin, nmax = (1 << 64) - 400_000, (1 << 64) - 1, 1000, 1333
+    want = orc.run(pmin, pmax, nmin, nmax)
+    lines = fs.SieveResult(want["factors"], want["checksum"], want["primecount"], want["factorcount"]).lines()
+    r = _cli(fslib, ["-n", str(nmin), "-N", str(nmax), "-p", str(pmin), "-P", "18446744073709551615", "-v", "4"],
+             tmp_path)
+    assert r.returncode == 0, r.stdout + r.stderr
+    got = (tmp_path / "factors.txt").read_text().splitlines()
+    assert got == (lines or ["no factors"]) + [f"{want['checksum']:016X}"]
+    assert f"prime count {want['primecount']}," in r.stdout

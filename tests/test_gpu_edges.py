@@ -1,0 +1,112 @@
+"""Edge cases and failure paths on the GPU, through the C ABI.
+
+Empty p- and n-ranges, a candidate buffer too small for its segment (the
+true count is still reported and the overflow is flagged, never silently
+truncated), and the plan check for a caller-supplied setup plan: a correct
+plan multiplies to nmin! mod p, a corrupted one raises FS_FLAG_TABLE.
+All comparisons are exact.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _counters(ctr):
+    import factsieve_gb300 as fs
+    return np.frombuffer(ctr.cpu().numpy().tobytes(), dtype=fs.COUNTERS_DTYPE)[0]
+
+
+def _plan_on_device(fs, nmin):
+    import torch
+    words, layers, deficit = fs.setup_plan(nmin)
+    words = np.concatenate([words, np.zeros(1, np.uint64)])   # d_words is non-null even when 2! needs no word
+    dw = torch.from_numpy(words.view(np.int64).copy()).cuda()
+    dl = torch.from_numpy(layers.astype(np.uint32).reshape(-1).view(np.int32).copy()).cuda()
+    return dw, dl, len(layers), deficit
+
+
+def _candidates(ctx, lo, hi):
+    import torch
+    import factsieve_gb300 as fs
+    cap = fs.candidate_capacity(lo, hi)
+    cand = torch.zeros(cap, dtype=torch.int64, device="cuda")
+    ctr = torch.zeros(4, dtype=torch.int64, device="cuda")
+    ctx.getsegprimes(lo, hi, cand.data_ptr(), cap, ctr.data_ptr())
+    return cand, ctr
+
+
+def test_empty_p_range(ctx):
+    r = ctx.sieve(10**12, 10**12, 1000, 2000)
+    assert (r.primecount, r.factorcount, r.checksum, len(r.factors)) == (0, 0, 0, 0)
+    # a range holding no candidate: 1e12+1..1e12+9 has no number free of factors <= 113 that is a 2-PRP
+    r = ctx.sieve(10**12 + 1, 10**12 + 10, 1000, 2000)
+    assert r.primecount == 0 and r.checksum == 0
+
+
+@pytest.mark.parametrize("lo,hi,n", [(1_000_000, 1_100_000, 1000), (10**12, 10**12 + 200_000, 100_000)])
+def test_empty_n_range_matches_oracle(ctx, orc, lo, hi, n):
+    """nmin == nmax walks no step; the checksum is still sum(nmin! R + nmax R) over the candidates."""
+    want = orc.run(lo, hi, n, n)
+    r = ctx.sieve(lo, hi, n, n)
+    assert (r.primecount, r.checksum, r.factorcount) == (want["primecount"], want["checksum"], 0)
+
+
+@pytest.mark.parametrize("nmin", [1, 2, 3, 4, 5, 6, 20, 33])
+def test_smallest_nmin_is_exact(ctx, orc, nmin):
+    """Below nmin = 34 the reference's setup (nmin < 4) or verifier (hits with
+    n < 34) is wrong, so the definition itself is the oracle here."""
+    want = orc.exact_small(127, 60_000, nmin, 400)
+    r = ctx.sieve(127, 60_000, nmin, 400)
+    assert (r.primecount, r.raw_sum, r.checksum, r.factorcount) == \
+        (want["primecount"], want["raw_sum"], want["checksum"], want["factorcount"])
+    assert [(int(p), int(nc)) for p, nc in zip(r.factors["p"], r.factors["nc"])] == want["factors"]
+
+
+def test_candidate_overflow_is_counted_and_flagged(ctx, orc):
+    import torch
+    import factsieve_gb300 as fs
+    lo, hi, cap = 1_000_000, 1_200_000, 10
+    cand = torch.zeros(cap, dtype=torch.int64, device="cuda")
+    res = torch.zeros(cap, dtype=torch.int64, device="cuda")
+    ctr = torch.zeros(4, dtype=torch.int64, device="cuda")
+    ctx.getsegprimes(lo, hi, cand.data_ptr(), cap, ctr.data_ptr())
+    want = orc.candidates(lo, hi)
+    c = _counters(ctr)
+    assert int(c["ncand"]) == len(want) > cap         # the true count, not the capacity
+    got = set(cand.cpu().numpy().view(np.uint64).tolist())
+    assert got <= set(int(x) for x in want)           # the slots that fit hold real candidates
+    ctx.setup(cand.data_ptr(), cap, ctr.data_ptr(), 1000, res.data_ptr())
+    ctx.check(cand.data_ptr(), cap, ctr.data_ptr(), res.data_ptr(), 1000)
+    assert int(_counters(ctr)["flags"]) & fs.FLAG_CAND_OVERFLOW
+
+
+@pytest.mark.parametrize("nmin", [2, 127, 100_000, 3_000_000])
+def test_plan_check_accepts_the_library_plan(ctx, nmin):
+    import factsieve_gb300 as fs
+    cand, ctr = _candidates(ctx, 1_000_000_000_039, 1_000_000_100_000)
+    dw, dl, nl, deficit = _plan_on_device(fs, nmin)
+    direct, table = ctx.plan_check(cand.data_ptr(), ctr.data_ptr(), nmin, dw.data_ptr(), dl.data_ptr(), nl, deficit)
+    assert direct == table
+    assert int(_counters(ctr)["flags"]) == 0
+    # the same value the library's own plan gives
+    assert ctx.table_check(cand.data_ptr(), ctr.data_ptr(), nmin) == (direct, table)
+
+
+@pytest.mark.parametrize("what", ["word", "deficit", "nmin"])
+def test_plan_check_flags_a_corrupted_plan(ctx, what):
+    import factsieve_gb300 as fs
+    nmin = 100_000
+    cand, ctr = _candidates(ctx, 1_000_000_000_039, 1_000_000_100_000)
+    dw, dl, nl, deficit = _plan_on_device(fs, nmin)
+    n_check = nmin
+    if what == "word":
+        dw[(len(dw) - 1) // 2] += 2      # one packed word of the product changed
+    elif what == "deficit":
+        deficit += 1
+    else:
+        n_check = nmin + 1               # the plan of nmin checked against (nmin+1)!
+    direct, table = ctx.plan_check(cand.data_ptr(), ctr.data_ptr(), n_check, dw.data_ptr(), dl.data_ptr(), nl,
+                                   deficit)
+    assert direct != table
+    assert int(_counters(ctr)["flags"]) & fs.FLAG_TABLE

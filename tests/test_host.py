@@ -29,7 +29,8 @@ def test_power_table_equals_oracle(fslib, orc):
             assert x.tolist() == y.tolist(), n
 
 
-@pytest.mark.parametrize("n,chunks", [(127, 1), (1000, 1), (4999, 1), (4999, 3), (20_000, 7), (2, 1), (1, 1)])
+@pytest.mark.parametrize("n,chunks", [(127, 1), (1000, 1), (4999, 1), (4999, 3), (20_000, 7), (1, 1), (2, 1), (3, 1),
+                                     (4, 1), (5, 2), (6, 1), (7, 3), (8, 1)])
 def test_setup_plan_multiplies_to_factorial(fslib, n, chunks):
     """Horner over each chunk's layers (square, double, multiply words) multiplies to
     exactly n!, and each chunk's deficit counts one R^-1 per word, doubled by

@@ -181,3 +181,27 @@ def test_oracle_hits_verify_with_reference(orc, refmath):
     assert len(out["hits"]) > 100
     for p, nc in zip(out["hits"]["p"].tolist(), out["hits"]["nc"].tolist()):
         assert refmath.verify(p, abs(nc), -1 if nc < 0 else 1)
+
+
+@pytest.mark.parametrize("nmin,nmax", [(34, 400), (127, 900), (300, 301)])
+def test_exact_definition_equals_restatement_where_the_reference_is_valid(orc, nmin, nmax):
+    """From nmin = 34 up the pure-Python definition and the reference restatement agree bit for bit."""
+    e = orc.exact_small(127, 60_000, nmin, nmax)
+    r = orc.run(127, 60_000, nmin, nmax)
+    assert r["status"] == 0
+    assert (e["primecount"], e["raw_sum"], e["checksum"], e["factorcount"]) == \
+        (r["primecount"], r["raw_sum"], r["checksum"], r["factorcount"])
+    assert e["factors"] == [(int(p), int(nc)) for p, nc in zip(r["factors"]["p"], r["factors"]["nc"])]
+
+
+def test_reference_is_invalid_below_nmin_34(orc):
+    """The domain edge the GPU path treats exactly: nmin 2 and 3 start from a wrong
+    residue in the reference (getPower's curBit for exponent 1) and hits with
+    n < 34 fail its verifier, which starts from 34!."""
+    e = orc.exact_small(127, 60_000, 3, 400)
+    r = orc.run(127, 60_000, 3, 400)
+    assert r["raw_sum"] != e["raw_sum"]
+    assert orc.run(127, 60_000, 20, 400)["status"] == -1          # a true factor with n < 34 rejected
+    assert orc.exact_small(127, 60_000, 20, 400)["raw_sum"] == orc.run(127, 60_000, 20, 400)["raw_sum"]
+    import math
+    assert (math.factorial(25) - 1) % 149 == 0 and not orc.verify(149, 25, -1)   # 149 | 25! - 1, rejected
