@@ -417,4 +417,84 @@ __device__ __forceinline__ u32 canon96_walk8x2(u32& al, u32& ah, u32& bl, u32& b
     return flag;
 }
 
+// ------------------------- iterate: lazy 64-bit steps, half-offset form --
+//
+// The lazy 64-bit step with the residue held as n! x mod p for
+// x = (p - 1)/2 = -1/2 mod p instead of n! R.  Then n! = +1 gives x and
+// n! = -1 gives -x = x + 1, two adjacent values.  The quotient estimate of
+// the lazy step falls short of floor(t/p) by at most one, and only when
+// t mod p < d p with d < 2^32/p + z/2^32 (z = t >> 32): the step leaves r in
+// [0, (1 + d) p).  For p >= 2^36 and p kmax <= 2^60 (r < 2p, z < 2p kmax /
+// 2^32) d < 1/16 + 1/8 < 1/2, so r never reaches x + p or x + 1 + p and the
+// exact hit test is r in {x, x + 1}: two compares of the low word per step
+// instead of the four the [0, 2p) window needs.
+struct Half64 {
+    u64 p, x;                 // x = (p - 1) / 2
+    u32 np0, np1, M;          // 2^64 - p (two words), floor(2^64 / p)
+    u32 x0, x1;               // low words of x and x + 1
+};
+
+__device__ __forceinline__ bool half_ok(u64 p, u32 kmax) {
+    return p >= (1ull << 36) && p <= ((1ull << 60) / (u64)(kmax ? kmax : 1));
+}
+
+__device__ __forceinline__ Half64 make_half(const Prime& c) {
+    Half64 H;
+    H.p = c.p;
+    H.x = (c.p - 1) >> 1;
+    const u64 np = 0ull - c.p;
+    H.np0 = (u32)np;
+    H.np1 = (u32)(np >> 32);
+    H.M = (u32)((~0ull) / c.p);
+    H.x0 = (u32)H.x;
+    H.x1 = (u32)(H.x + 1);
+    return H;
+}
+
+// n! R (canonical) -> n! x, and back: x R^-1 by one Montgomery product with
+// x, and x^-1 = -2 by one with -2 R^2.
+__device__ __forceinline__ u64 half_enter(u64 r, const Prime& c, const Half64& H) {
+    return mont_mul(r, H.x, c.p, c.pinv);
+}
+__device__ __forceinline__ u64 half_leave(u64 r, const Prime& c) {
+    const u64 two_r2 = mod_add(c.r2, c.r2, c.p);
+    return mont_mul(r, c.p - two_r2, c.p, c.pinv);
+}
+
+__device__ __forceinline__ u64 half_step(u64 r, u32 k, const Half64& H) {
+    const u64 t = r * (u64)k;
+    const u32 qe = __umulhi((u32)(t >> 32), H.M);
+    return t + (u64)qe * (((u64)H.np1 << 32) | H.np0);
+}
+__device__ __forceinline__ u64 half_canon(u64 r, const Half64& H) { return r >= H.p ? r - H.p : r; }
+
+#define FS_HF_TEST(RL, X0, X1)                         \
+    "setp.eq.or.u32 P, " RL ", " X0 ", P;\n\t"         \
+    "setp.eq.or.u32 P, " RL ", " X1 ", P;\n\t"
+#define FS_HF_STEP2(J)                                              \
+    "add.u32 kk, %5, " #J ";\n\t"                                   \
+    FS_HF_TEST("%0", "%9", "%10")                                   \
+    FS_HF_TEST("%2", "%14", "%15")                                  \
+    FS_LZ_MUL("%0", "%1", "%6", "%7", "%8", "TA", "RA", "aL", "aH", "qA") \
+    FS_LZ_MUL("%2", "%3", "%11", "%12", "%13", "TB", "RB", "bL", "bH", "qB")
+
+// Eight half-offset steps on two residues; the flag as lazy_walk8x2's.
+__device__ __forceinline__ u32 half_walk8x2(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const Half64& A,
+                                            const Half64& B) {
+    u32 flag;
+    asm("{\n\t"
+        ".reg .u32 kk, aL, aH, qA, bL, bH, qB;\n\t"
+        ".reg .u64 TA, RA, TB, RB;\n\t"
+        ".reg .pred P;\n\t"
+        "setp.ne.u32 P, %5, %5;\n\t"
+        FS_HF_STEP2(0) FS_HF_STEP2(1) FS_HF_STEP2(2) FS_HF_STEP2(3)
+        FS_HF_STEP2(4) FS_HF_STEP2(5) FS_HF_STEP2(6) FS_HF_STEP2(7)
+        "selp.u32 %4, 1, 0, P;\n\t"
+        "}"
+        : "+r"(al), "+r"(ah), "+r"(bl), "+r"(bh), "=r"(flag)
+        : "r"(k1), "r"(A.np0), "r"(A.np1), "r"(A.M), "r"(A.x0), "r"(A.x1), "r"(B.np0), "r"(B.np1), "r"(B.M),
+          "r"(B.x0), "r"(B.x1));
+    return flag;
+}
+
 }  // namespace fs

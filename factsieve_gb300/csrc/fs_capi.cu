@@ -161,13 +161,29 @@ fs::SieveArgs base_args(PlanGPU* pl) {
     return a;
 }
 
+// Sieve kernel build (fs_tuning.sieve_variant): 2..4 two candidates per
+// thread at that many resident blocks per SM, 5 / 6 four candidates per
+// thread at 2 / 3.  The default is 5, which the measurements favour on every
+// segment whose candidates share one walk step (the usual case).
 int variant(fs_ctx* c) {
     const uint32_t v = c->tuning.sieve_variant;
-    return (v == 2 || v == 3 || v == 4) ? (int)v : 3;
+    return (v >= 2 && v <= 6) ? (int)v : 5;
 }
 
-int sieve_grid(fs_ctx* c) {
-    int bpsm = c->tuning.sieve_blocks_per_sm ? (int)c->tuning.sieve_blocks_per_sm : c->sieve_occ[variant(c)];
+// The build a launch really runs: the four-candidate kernels exist for the
+// specialised walks only; a mixed segment (WALK_ANY) runs variant 3.
+int kernel_variant(int v, int walk) { return ((v == 5 || v == 6) && walk == fs::WALK_ANY) ? 3 : v; }
+
+// Default blocks per SM for a build: its resident occupancy, and for the
+// four-candidate builds four times that, so the candidates are dealt in
+// smaller shares and the last wave is short.
+int default_bpsm(fs_ctx* c, int kv) { return c->sieve_occ[kv] * ((kv == 5 || kv == 6) ? 4 : 1); }
+
+// The build for launches that walk each candidate with its own step.
+int any_variant(fs_ctx* c) { return kernel_variant(variant(c), fs::WALK_ANY); }
+
+int sieve_grid(fs_ctx* c, int kv) {
+    const int bpsm = c->tuning.sieve_blocks_per_sm ? (int)c->tuning.sieve_blocks_per_sm : default_bpsm(c, kv);
     return std::max(1, c->sm_count * bpsm);
 }
 
@@ -279,7 +295,6 @@ int run_sieve(fs_ctx* c, const u64* d_cand, uint32_t cap, fs::Counters* d_ctr, u
     if (split) {
         if ((rc = grow(c, &c->d_residue, &c->residue_cap, (uint64_t)cap + 1))) return rc;
     }
-    const int grid = sieve_grid(c);
     fs::SieveArgs a = base_args(pl);
     a.cand = d_cand;
     a.ncand = &d_ctr->ncand;
@@ -292,7 +307,7 @@ int run_sieve(fs_ctx* c, const u64* d_cand, uint32_t cap, fs::Counters* d_ctr, u
     if (chunks > 1) {
         if ((rc = grow(c, &c->d_partials, &c->partials_cap, (uint64_t)cap * chunks + 1))) return rc;
         a.partials = c->d_partials;
-        int gx = std::max(1, sieve_grid(c) / (int)chunks);
+        int gx = std::max(1, sieve_grid(c, any_variant(c)) / (int)chunks);
         std::pair<cudaEvent_t, cudaEvent_t> ev;
         if ((rc = ev_begin(c, &ev))) return rc;
         CK(c, fs::launch_setup_partial(a, gx, (int)chunks, c->stream));
@@ -314,7 +329,8 @@ int run_sieve(fs_ctx* c, const u64* d_cand, uint32_t cap, fs::Counters* d_ctr, u
         a.store_final = 0;
         std::pair<cudaEvent_t, cudaEvent_t> ev;
         if ((rc = ev_begin(c, &ev))) return rc;
-        CK(c, fs::launch_sieve(a, first ? setup_mode : fs::SETUP_LOAD, fin, grid, c->stream, variant(c), walk));
+        const int kv = kernel_variant(variant(c), walk);
+        CK(c, fs::launch_sieve(a, first ? setup_mode : fs::SETUP_LOAD, fin, sieve_grid(c, kv), c->stream, kv, walk));
         if ((rc = ev_end(c, ev, c->sieve_ev))) return rc;
         ++c->launches;
         ++c->sieve_launches;
@@ -391,7 +407,7 @@ int fs_create(int device, fs_ctx** out) {
     cudaDeviceGetAttribute(&clk, cudaDevAttrClockRate, device);
     c->clock_khz = clk;
     c->total_mem = prop.totalGlobalMem;
-    for (int v = 2; v <= 4; ++v) {
+    for (int v = 2; v <= 6; ++v) {
         int occ = 0;
         if (fs::sieve_occupancy(&occ, v) == cudaSuccess && occ > 0) c->sieve_occ[v] = occ;
     }
@@ -482,7 +498,7 @@ int fs_get_tuning(fs_ctx* c, fs_tuning* t) {
     if (!c || !t) return FS_E_ARG;
     *t = c->tuning;
     if (!t->sieve_variant) t->sieve_variant = (uint32_t)variant(c);
-    if (!t->sieve_blocks_per_sm) t->sieve_blocks_per_sm = (uint32_t)c->sieve_occ[variant(c)];
+    if (!t->sieve_blocks_per_sm) t->sieve_blocks_per_sm = (uint32_t)default_bpsm(c, variant(c));
     return FS_OK;
 }
 
@@ -636,10 +652,10 @@ int fs_setup(fs_ctx* c, const uint64_t* d_cand, uint32_t cap, fs_counters* d_ctr
     if (chunks > 1) {
         if ((rc = grow(c, &c->d_partials, &c->partials_cap, (uint64_t)cap * chunks + 1))) return rc;
         a.partials = c->d_partials;
-        CK(c, fs::launch_setup_partial(a, std::max(1, sieve_grid(c) / (int)chunks), (int)chunks, c->stream));
+        CK(c, fs::launch_setup_partial(a, std::max(1, sieve_grid(c, any_variant(c)) / (int)chunks), (int)chunks, c->stream));
         mode = fs::SETUP_PARTIALS;
     }
-    CK(c, fs::launch_sieve(a, mode, false, sieve_grid(c), c->stream, variant(c), fs::WALK_ANY));
+    CK(c, fs::launch_sieve(a, mode, false, sieve_grid(c, any_variant(c)), c->stream, any_variant(c), fs::WALK_ANY));
     return FS_OK;
 }
 
@@ -663,7 +679,7 @@ int fs_iterate(fs_ctx* c, const uint64_t* d_cand, uint32_t cap, fs_counters* d_c
         uint32_t e = (maxs && nend - s > maxs) ? s + maxs : nend;
         a.nstart = s;
         a.nend = e;
-        CK(c, fs::launch_sieve(a, fs::SETUP_LOAD, false, sieve_grid(c), c->stream, variant(c), fs::WALK_ANY));
+        CK(c, fs::launch_sieve(a, fs::SETUP_LOAD, false, sieve_grid(c, any_variant(c)), c->stream, any_variant(c), fs::WALK_ANY));
         s = e;
     } while (s < nend);
     return FS_OK;
@@ -684,7 +700,7 @@ int fs_check(fs_ctx* c, const uint64_t* d_cand, uint32_t cap, fs_counters* d_ctr
     a.nmax = nmax;
     a.count_candidates = 1;
     a.store_final = 0;
-    CK(c, fs::launch_sieve(a, fs::SETUP_LOAD, true, sieve_grid(c), c->stream, variant(c), fs::WALK_ANY));
+    CK(c, fs::launch_sieve(a, fs::SETUP_LOAD, true, sieve_grid(c, any_variant(c)), c->stream, any_variant(c), fs::WALK_ANY));
     return FS_OK;
 }
 

@@ -33,7 +33,7 @@ struct fs_ctx {
     cudaStream_t own = nullptr, stream = nullptr;
     int sm_count = 0, clock_khz = 0;
     uint64_t total_mem = 0;
-    int sieve_occ[5] = {1, 1, 1, 1, 1};
+    int sieve_occ[7] = {1, 1, 1, 1, 1, 1, 1};
     fs_tuning tuning{};
     std::string err;
     // search state

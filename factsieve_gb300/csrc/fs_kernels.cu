@@ -209,6 +209,43 @@ __device__ __forceinline__ void plan_product2(const Prime& a, const Prime& b, co
     xb = y;
 }
 
+// The same for four candidates: four independent product chains per table
+// load, for the four-candidate sieve kernel.
+__device__ __forceinline__ void plan_product4(const Prime (&c)[4], const u64* __restrict__ words,
+                                              const Layer* __restrict__ layers, u32 lb, u32 le, u64 (&x)[4]) {
+#pragma unroll
+    for (int h = 0; h < 4; ++h) x[h] = c[h].one;
+    for (u32 l = lb; l < le; ++l) {
+        const Layer L = layers[l];
+        if (l != lb) {
+#pragma unroll
+            for (int h = 0; h < 4; ++h) x[h] = mont_mul(x[h], x[h], c[h].p, c[h].pinv);
+        }
+        if (L.dbl) {
+#pragma unroll
+            for (int h = 0; h < 4; ++h) x[h] = mod_add(x[h], x[h], c[h].p);
+        }
+        u32 i = L.begin;
+        if ((i & 1) && i < L.end) {
+            const u64 w = __ldg(words + i++);
+#pragma unroll
+            for (int h = 0; h < 4; ++h) x[h] = mont_mul(x[h], w, c[h].p, c[h].pinv);
+        }
+        for (; i + 2 <= L.end; i += 2) {
+            const ulonglong2 w2 = __ldg(reinterpret_cast<const ulonglong2*>(words + i));
+#pragma unroll
+            for (int h = 0; h < 4; ++h) x[h] = mont_mul(x[h], w2.x, c[h].p, c[h].pinv);
+#pragma unroll
+            for (int h = 0; h < 4; ++h) x[h] = mont_mul(x[h], w2.y, c[h].p, c[h].pinv);
+        }
+        if (i < L.end) {
+            const u64 w = __ldg(words + i);
+#pragma unroll
+            for (int h = 0; h < 4; ++h) x[h] = mont_mul(x[h], w, c[h].p, c[h].pinv);
+        }
+    }
+}
+
 struct WalkOut {
     HitStage* st;
     Factor* hits;
@@ -217,7 +254,10 @@ struct WalkOut {
     int tag;   // stored in each hit record's pad word (job index in a batch, else 0)
 };
 
-// The three Barrett walk regimes behind one interface.
+// The Barrett walk regimes behind one interface.  enter / leave convert a
+// canonical n! R into the regime's residue form and back; hit classifies a
+// canonical residue of that form: -1 for n! = 1 (p | n! - 1), +1 for n! = -1
+// (p | n! + 1), 0 for neither.
 struct RegT64 {
     using K = Lazy64;
     static __device__ __forceinline__ K make(const Prime& c, u32) { return make_lazy(c); }
@@ -226,6 +266,11 @@ struct RegT64 {
     }
     static __device__ __forceinline__ u64 step(u64 r, u32 k, const K& X) { return lazy_step(r, k, X); }
     static __device__ __forceinline__ u64 canon(u64 r, const K& X) { return lazy_canon(r, X); }
+    static __device__ __forceinline__ u64 enter(u64 r, const Prime&, const K&) { return r; }
+    static __device__ __forceinline__ u64 leave(u64 r, const Prime&, const K& X) { return lazy_canon(r, X); }
+    static __device__ __forceinline__ int hit(u64 c, const K& X) {
+        return c == X.one ? -1 : (c == X.p - X.one ? 1 : 0);
+    }
 };
 struct RegL96 {
     using K = Lazy96;
@@ -235,6 +280,11 @@ struct RegL96 {
     }
     static __device__ __forceinline__ u64 step(u64 r, u32 k, const K& X) { return lazy96_step(r, k, X); }
     static __device__ __forceinline__ u64 canon(u64 r, const K& X) { return lazy96_canon(r, X); }
+    static __device__ __forceinline__ u64 enter(u64 r, const Prime&, const K&) { return r; }
+    static __device__ __forceinline__ u64 leave(u64 r, const Prime&, const K& X) { return lazy96_canon(r, X); }
+    static __device__ __forceinline__ int hit(u64 c, const K& X) {
+        return c == X.one ? -1 : (c == X.p - X.one ? 1 : 0);
+    }
 };
 struct RegC96 {
     using K = Canon96;
@@ -244,14 +294,32 @@ struct RegC96 {
     }
     static __device__ __forceinline__ u64 step(u64 r, u32 k, const K& X) { return canon96_step(r, k, X); }
     static __device__ __forceinline__ u64 canon(u64 r, const K&) { return r; }
+    static __device__ __forceinline__ u64 enter(u64 r, const Prime&, const K&) { return r; }
+    static __device__ __forceinline__ u64 leave(u64 r, const Prime&, const K&) { return r; }
+    static __device__ __forceinline__ int hit(u64 c, const K& X) {
+        return c == X.one ? -1 : (c == X.p - X.one ? 1 : 0);
+    }
+};
+struct RegH64 {
+    using K = Half64;
+    static __device__ __forceinline__ K make(const Prime& c, u32) { return make_half(c); }
+    static __device__ __forceinline__ u32 block(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const K& A, const K& B) {
+        return half_walk8x2(al, ah, bl, bh, k1, A, B);
+    }
+    static __device__ __forceinline__ u64 step(u64 r, u32 k, const K& X) { return half_step(r, k, X); }
+    static __device__ __forceinline__ u64 canon(u64 r, const K& X) { return half_canon(r, X); }
+    static __device__ __forceinline__ u64 enter(u64 r, const Prime& c, const K& X) { return half_enter(r, c, X); }
+    static __device__ __forceinline__ u64 leave(u64 r, const Prime& c, const K& X) {
+        return half_leave(half_canon(r, X), c);
+    }
+    static __device__ __forceinline__ int hit(u64 c, const K& X) { return c == X.x ? -1 : (c == X.x + 1 ? 1 : 0); }
 };
 
 // Exact +-1 test of a walk residue at n, recording a hit.
 template <class Reg>
 __device__ __forceinline__ void reg_check(u64 r, u32 n, const typename Reg::K& X, const WalkOut& o) {
-    const u64 c = Reg::canon(r, X);
-    if (c == X.one || c == X.p - X.one)
-        record_hit(*o.st, X.p, c == X.one ? -(int)n : (int)n, o.hits, o.hitcap, o.ctr, o.tag);
+    const int h = Reg::hit(Reg::canon(r, X), X);
+    if (h) record_hit(*o.st, X.p, h * (int)n, o.hits, o.hitcap, o.ctr, o.tag);
 }
 
 // Replay eight steps from r at n0 with exact tests (the PTX block saw a
@@ -265,7 +333,8 @@ __device__ __noinline__ void reg_replay8(u64 r, u32 n0, typename Reg::K X, WalkO
 }
 
 // Walk two candidates of one regime over [nstart, nend); residues in and out
-// are canonical.  real_b = false: b duplicates a and its hits are dropped.
+// are in the regime's form (out not yet canonical).  real_b = false: b
+// duplicates a and its hits are dropped.
 template <class Reg>
 __device__ __forceinline__ void walk_reg2(u64& ra, u64& rb, const typename Reg::K& A, const typename Reg::K& B,
                                           bool real_b, u32 nstart, u32 nend, const WalkOut& o) {
@@ -287,8 +356,8 @@ __device__ __forceinline__ void walk_reg2(u64& ra, u64& rb, const typename Reg::
             b = Reg::step(b, n + 1, B);
         }
     }
-    ra = Reg::canon(a, A);
-    if (real_b) rb = Reg::canon(b, B);
+    ra = a;
+    if (real_b) rb = b;
 }
 
 template <class Reg>
@@ -296,9 +365,11 @@ __device__ __forceinline__ void walk_reg_pair(u64& ra, u64& rb, const Prime& a, 
                                               u32 nstart, u32 nend, const WalkOut& o) {
     const typename Reg::K A = Reg::make(a, nend);
     const typename Reg::K B = real_b ? Reg::make(b, nend) : A;
-    u64 rb2 = real_b ? rb : ra;
-    walk_reg2<Reg>(ra, rb2, A, B, real_b, nstart, nend, o);
-    if (real_b) rb = rb2;
+    u64 wa = Reg::enter(ra, a, A);
+    u64 wb = real_b ? Reg::enter(rb, b, B) : wa;
+    walk_reg2<Reg>(wa, wb, A, B, real_b, nstart, nend, o);
+    ra = Reg::leave(wa, a, A);
+    if (real_b) rb = Reg::leave(wb, b, B);
 }
 
 // Generic walk for any p < 2^64 and n < 2^31: multiply by the Montgomery
@@ -315,9 +386,11 @@ __device__ __forceinline__ u64 walk_generic(u64 r, const Prime& c, u32 nstart, u
     return r;
 }
 
-// Walk regime of one candidate for multipliers up to kmax: 1 lazy 64-bit,
-// 2 lazy 96-bit, 3 canonical 96-bit, 0 generic Montgomery.
+// Walk regime of one candidate for multipliers up to kmax: 4 lazy 64-bit in
+// half-offset form, 1 lazy 64-bit, 2 lazy 96-bit, 3 canonical 96-bit,
+// 0 generic Montgomery.
 __device__ __forceinline__ int walk_regime(u64 p, u32 kmax) {
+    if (half_ok(p, kmax)) return 4;
     if (lazy_ok(p, kmax)) return 1;
     if (lazy96_ok(p, kmax)) return 2;
     if (canon96_ok(p, kmax)) return 3;
@@ -330,6 +403,7 @@ __device__ __forceinline__ void walk_one(u64& r, const Prime& c, int reg, u32 ns
         case 1: walk_reg_pair<RegT64>(r, dup, c, c, false, nstart, nend, o); break;
         case 2: walk_reg_pair<RegL96>(r, dup, c, c, false, nstart, nend, o); break;
         case 3: walk_reg_pair<RegC96>(r, dup, c, c, false, nstart, nend, o); break;
+        case 4: walk_reg_pair<RegH64>(r, dup, c, c, false, nstart, nend, o); break;
         default: r = walk_generic(r, c, nstart, nend, o); break;
     }
 }
@@ -351,6 +425,7 @@ __device__ __forceinline__ void walk_pair(u64& ra, u64& rb, const Prime& a, cons
         switch (ga) {
             case 1: walk_reg_pair<RegT64>(ra, rb, a, b, real_b, nstart, nend, o); return;
             case 2: walk_reg_pair<RegL96>(ra, rb, a, b, real_b, nstart, nend, o); return;
+            case 4: walk_reg_pair<RegH64>(ra, rb, a, b, real_b, nstart, nend, o); return;
             default: walk_reg_pair<RegC96>(ra, rb, a, b, real_b, nstart, nend, o); return;
         }
     }
@@ -362,10 +437,89 @@ template <int WALK>
 __device__ __forceinline__ void walk_pair_as(u64& ra, u64& rb, const Prime& a, const Prime& b, bool real_b,
                                              u32 nstart, u32 nend, const WalkOut& o) {
     if (nstart >= nend) return;
-    if (WALK == WALK_T64) walk_reg_pair<RegT64>(ra, rb, a, b, real_b, nstart, nend, o);
+    if (WALK == WALK_H64) walk_reg_pair<RegH64>(ra, rb, a, b, real_b, nstart, nend, o);
+    else if (WALK == WALK_T64) walk_reg_pair<RegT64>(ra, rb, a, b, real_b, nstart, nend, o);
     else if (WALK == WALK_L96) walk_reg_pair<RegL96>(ra, rb, a, b, real_b, nstart, nend, o);
     else if (WALK == WALK_C96) walk_reg_pair<RegC96>(ra, rb, a, b, real_b, nstart, nend, o);
     else walk_pair(ra, rb, a, b, real_b, nstart, nend, o);
+}
+
+// Walk four candidates of one regime over [nstart, nend) as two pairs whose
+// PTX blocks have no dependence on each other, so four residue chains are in
+// flight per thread.  Candidates h >= nreal duplicate candidate 0: they are
+// walked (the warp stays converged) but never tested or returned.
+//
+// The candidates' Montgomery constants are not kept across the walk (they
+// would cost the registers that a third resident block needs): c is rebuilt
+// from p after it, for leave() and the caller's final check.
+template <class Reg>
+__device__ __forceinline__ void walk_reg4(u64 (&r)[4], Prime (&c)[4], u32 nreal, u32 nstart, u32 nend,
+                                          const WalkOut& o) {
+    const typename Reg::K K0 = Reg::make(c[0], nend), K1 = Reg::make(c[1], nend);
+    const typename Reg::K K2 = Reg::make(c[2], nend), K3 = Reg::make(c[3], nend);
+    const u64 w0 = Reg::enter(r[0], c[0], K0), w1 = Reg::enter(r[1], c[1], K1);
+    const u64 w2 = Reg::enter(r[2], c[2], K2), w3 = Reg::enter(r[3], c[3], K3);
+    u32 l0 = (u32)w0, h0 = (u32)(w0 >> 32), l1 = (u32)w1, h1 = (u32)(w1 >> 32);
+    u32 l2 = (u32)w2, h2 = (u32)(w2 >> 32), l3 = (u32)w3, h3 = (u32)(w3 >> 32);
+    u32 n = nstart;
+    for (; n + 8 <= nend; n += 8) {
+        const u64 s0 = ((u64)h0 << 32) | l0, s1 = ((u64)h1 << 32) | l1;
+        const u64 s2 = ((u64)h2 << 32) | l2, s3 = ((u64)h3 << 32) | l3;
+        const u32 f1 = Reg::block(l0, h0, l1, h1, n + 1, K0, K1);
+        const u32 f2 = Reg::block(l2, h2, l3, h3, n + 1, K2, K3);
+        if (f1 | f2) {
+            if (f1) {
+                reg_replay8<Reg>(s0, n, K0, o);
+                if (nreal > 1) reg_replay8<Reg>(s1, n, K1, o);
+            }
+            if (f2 && nreal > 2) {
+                reg_replay8<Reg>(s2, n, K2, o);
+                if (nreal > 3) reg_replay8<Reg>(s3, n, K3, o);
+            }
+        }
+    }
+    u64 x0 = ((u64)h0 << 32) | l0, x1 = ((u64)h1 << 32) | l1;
+    u64 x2 = ((u64)h2 << 32) | l2, x3 = ((u64)h3 << 32) | l3;
+    for (; n < nend; ++n) {
+        reg_check<Reg>(x0, n, K0, o);
+        x0 = Reg::step(x0, n + 1, K0);
+        if (nreal > 1) {
+            reg_check<Reg>(x1, n, K1, o);
+            x1 = Reg::step(x1, n + 1, K1);
+        }
+        if (nreal > 2) {
+            reg_check<Reg>(x2, n, K2, o);
+            x2 = Reg::step(x2, n + 1, K2);
+        }
+        if (nreal > 3) {
+            reg_check<Reg>(x3, n, K3, o);
+            x3 = Reg::step(x3, n + 1, K3);
+        }
+    }
+    c[0] = make_prime(K0.p);
+    c[1] = make_prime(K1.p);
+    c[2] = make_prime(K2.p);
+    c[3] = make_prime(K3.p);
+    r[0] = Reg::leave(x0, c[0], K0);
+    if (nreal > 1) r[1] = Reg::leave(x1, c[1], K1);
+    if (nreal > 2) r[2] = Reg::leave(x2, c[2], K2);
+    if (nreal > 3) r[3] = Reg::leave(x3, c[3], K3);
+}
+
+// Four candidates with a step valid for all of them (WALK_T64 / WALK_L96 /
+// WALK_C96), or, for WALK_ANY, as two pairs one after the other.
+template <int WALK>
+__device__ __forceinline__ void walk_quad_as(u64 (&r)[4], Prime (&c)[4], u32 nreal, u32 nstart, u32 nend,
+                                             const WalkOut& o) {
+    if (nstart >= nend) return;
+    if (WALK == WALK_H64) walk_reg4<RegH64>(r, c, nreal, nstart, nend, o);
+    else if (WALK == WALK_T64) walk_reg4<RegT64>(r, c, nreal, nstart, nend, o);
+    else if (WALK == WALK_L96) walk_reg4<RegL96>(r, c, nreal, nstart, nend, o);
+    else if (WALK == WALK_C96) walk_reg4<RegC96>(r, c, nreal, nstart, nend, o);
+    else {
+        walk_pair(r[0], r[1], c[0], c[1], nreal > 1, nstart, nend, o);
+        if (nreal > 2) walk_pair(r[2], r[3], c[2], c[3], nreal > 3, nstart, nend, o);
+    }
 }
 
 // Starting residue of candidate i (SETUP mode), before the walk.
@@ -385,7 +539,7 @@ __device__ __forceinline__ u64 start_residue_one(const SieveArgs& a, const Prime
     return r;
 }
 
-template <int SETUP, bool FINAL, int MINB, int WALK>
+template <int SETUP, bool FINAL, int MINB, int WALK, int PPT>
 __global__ void __launch_bounds__(kSieveThreads, MINB) sieve_kernel(SieveArgs a) {
     __shared__ HitStage st;
     __shared__ u64 wsum[kSieveThreads / 32];
@@ -397,8 +551,46 @@ __global__ void __launch_bounds__(kSieveThreads, MINB) sieve_kernel(SieveArgs a)
     const WalkOut o{&st, a.hits, a.hitcap, a.ctr, 0};
     u64 sum = 0;
     u32 bad = 0;
-    const u32 npairs = (n + 1) / 2;
     const u32 stride = gridDim.x * blockDim.x;
+    if constexpr (PPT == 4) {
+        // four candidates per thread: two interleaved pairs
+        const u32 nquads = (n + 3) / 4;
+        for (u32 j = blockIdx.x * blockDim.x + threadIdx.x; j < nquads; j += stride) {
+            const u32 i0 = 4 * j;
+            const u32 nreal = n - i0 < 4 ? n - i0 : 4;
+            Prime c[4];
+            c[0] = make_prime(a.cand[i0]);
+#pragma unroll
+            for (int h = 1; h < 4; ++h) c[h] = (u32)h < nreal ? make_prime(a.cand[i0 + h]) : c[0];
+            u64 r[4];
+            if (SETUP == SETUP_PLAN) {
+                plan_product4(c, a.plan.words, a.plan.layers, a.plan.layer_begin, a.plan.layer_end, r);
+#pragma unroll
+                for (int h = 0; h < 4; ++h)
+                    r[h] = mont_mul(r[h], mont_pow(c[h].r2, a.plan.deficit, c[h]), c[h].p, c[h].pinv);
+            } else {
+                r[0] = start_residue_one<SETUP>(a, c[0], i0);
+#pragma unroll
+                for (int h = 1; h < 4; ++h) r[h] = (u32)h < nreal ? start_residue_one<SETUP>(a, c[h], i0 + h) : r[0];
+            }
+            walk_quad_as<WALK>(r, c, nreal, a.nstart, a.nend, o);
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {
+                if ((u32)h >= nreal) break;
+                if (FINAL) {
+                    const u64 s7 = to_mont(a.nmax, c[h]);
+                    u32 back = (u32)mont_mul(s7, 1, c[h].p, c[h].pinv);
+                    if (c[h].p <= a.nmax && a.nmax % c[h].p == back) back = a.nmax;
+                    bad += back != a.nmax;
+                    sum += r[h] + s7;
+                    if (a.store_final) a.residue[i0 + h] = r[h];
+                } else {
+                    a.residue[i0 + h] = r[h];
+                }
+            }
+        }
+    } else {
+    const u32 npairs = (n + 1) / 2;
     for (u32 j = blockIdx.x * blockDim.x + threadIdx.x; j < npairs; j += stride) {
         const u32 ia = 2 * j, ib = 2 * j + 1;
         const bool real_b = ib < n;
@@ -435,6 +627,7 @@ __global__ void __launch_bounds__(kSieveThreads, MINB) sieve_kernel(SieveArgs a)
             a.residue[ia] = ra;
             if (real_b) a.residue[ib] = rb;
         }
+    }
     }
     if (FINAL) {
         // warp then block reduction of the checksum, one atomic per block
@@ -821,18 +1014,18 @@ cudaError_t launch_gen(const GenArgs& a, int grid, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-template <int MINB, int WALK>
+template <int MINB, int WALK, int PPT = 2>
 static void launch_sieve_w(const SieveArgs& a, int setup, bool fin, int grid, cudaStream_t s) {
     const int t = kSieveThreads;
     if (setup == SETUP_PLAN) {
-        if (fin) sieve_kernel<SETUP_PLAN, true, MINB, WALK><<<grid, t, 0, s>>>(a);
-        else sieve_kernel<SETUP_PLAN, false, MINB, WALK><<<grid, t, 0, s>>>(a);
+        if (fin) sieve_kernel<SETUP_PLAN, true, MINB, WALK, PPT><<<grid, t, 0, s>>>(a);
+        else sieve_kernel<SETUP_PLAN, false, MINB, WALK, PPT><<<grid, t, 0, s>>>(a);
     } else if (setup == SETUP_PARTIALS) {
-        if (fin) sieve_kernel<SETUP_PARTIALS, true, MINB, WALK><<<grid, t, 0, s>>>(a);
-        else sieve_kernel<SETUP_PARTIALS, false, MINB, WALK><<<grid, t, 0, s>>>(a);
+        if (fin) sieve_kernel<SETUP_PARTIALS, true, MINB, WALK, PPT><<<grid, t, 0, s>>>(a);
+        else sieve_kernel<SETUP_PARTIALS, false, MINB, WALK, PPT><<<grid, t, 0, s>>>(a);
     } else {
-        if (fin) sieve_kernel<SETUP_LOAD, true, MINB, WALK><<<grid, t, 0, s>>>(a);
-        else sieve_kernel<SETUP_LOAD, false, MINB, WALK><<<grid, t, 0, s>>>(a);
+        if (fin) sieve_kernel<SETUP_LOAD, true, MINB, WALK, PPT><<<grid, t, 0, s>>>(a);
+        else sieve_kernel<SETUP_LOAD, false, MINB, WALK, PPT><<<grid, t, 0, s>>>(a);
     }
 }
 
@@ -846,8 +1039,22 @@ cudaError_t launch_sieve(const SieveArgs& a, int setup, bool final_chunk, int gr
         launch_sieve_w<2, WALK_ANY>(a, setup, final_chunk, grid, s);
     } else if (variant == 4) {
         launch_sieve_w<4, WALK_ANY>(a, setup, final_chunk, grid, s);
+    } else if (variant == 5 || variant == 6) {
+        // four candidates per thread, 2 (variant 5) or 3 (variant 6) blocks per SM
+        switch (walk * 2 + (variant == 6)) {
+            case WALK_H64 * 2: launch_sieve_w<2, WALK_H64, 4>(a, setup, final_chunk, grid, s); break;
+            case WALK_H64 * 2 + 1: launch_sieve_w<3, WALK_H64, 4>(a, setup, final_chunk, grid, s); break;
+            case WALK_T64 * 2: launch_sieve_w<2, WALK_T64, 4>(a, setup, final_chunk, grid, s); break;
+            case WALK_L96 * 2: launch_sieve_w<2, WALK_L96, 4>(a, setup, final_chunk, grid, s); break;
+            case WALK_C96 * 2: launch_sieve_w<2, WALK_C96, 4>(a, setup, final_chunk, grid, s); break;
+            case WALK_T64 * 2 + 1: launch_sieve_w<3, WALK_T64, 4>(a, setup, final_chunk, grid, s); break;
+            case WALK_L96 * 2 + 1: launch_sieve_w<3, WALK_L96, 4>(a, setup, final_chunk, grid, s); break;
+            case WALK_C96 * 2 + 1: launch_sieve_w<3, WALK_C96, 4>(a, setup, final_chunk, grid, s); break;
+            default: launch_sieve_w<3, WALK_ANY>(a, setup, final_chunk, grid, s); break;
+        }
     } else {
         switch (walk) {
+            case WALK_H64: launch_sieve_w<3, WALK_H64>(a, setup, final_chunk, grid, s); break;
             case WALK_T64: launch_sieve_w<3, WALK_T64>(a, setup, final_chunk, grid, s); break;
             case WALK_L96: launch_sieve_w<3, WALK_L96>(a, setup, final_chunk, grid, s); break;
             case WALK_C96: launch_sieve_w<3, WALK_C96>(a, setup, final_chunk, grid, s); break;
@@ -898,6 +1105,8 @@ int walk_for_range(uint64_t plo, uint64_t phi, uint32_t kmax) {
     if (phi <= plo || kmax == 0) return WALK_ANY;
     const uint64_t pmax = phi - 1;
     const int kb = 32 - __builtin_clz(kmax);
+    // the half-offset lazy step needs p >= 2^36 and p kmax <= 2^60 (half_ok)
+    if (plo >= (1ull << 36) && pmax <= ((1ull << 60) / kmax)) return WALK_H64;
     // the lazy 64-bit step needs p > 2^33 and p kmax <= 2^62 (lazy_ok)
     if (plo > (1ull << 33) && pmax <= ((1ull << 62) / kmax)) return WALK_T64;
     if (kb <= 28 && plo > (1ull << 33) && (pmax >> 63) == 0) return WALK_L96;
@@ -910,12 +1119,16 @@ int gen_threads() { return kGenWarps * 32; }
 
 cudaError_t sieve_occupancy(int* blocks_per_sm, int variant) {
     switch (variant) {
-        case 2: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, sieve_kernel<SETUP_PLAN, true, 2, WALK_ANY>,
-                                                                     kSieveThreads, 0);
-        case 4: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, sieve_kernel<SETUP_PLAN, true, 4, WALK_ANY>,
-                                                                     kSieveThreads, 0);
-        default: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, sieve_kernel<SETUP_PLAN, true, 3, WALK_ANY>,
-                                                                      kSieveThreads, 0);
+        case 2: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                    blocks_per_sm, sieve_kernel<SETUP_PLAN, true, 2, WALK_ANY, 2>, kSieveThreads, 0);
+        case 4: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                    blocks_per_sm, sieve_kernel<SETUP_PLAN, true, 4, WALK_ANY, 2>, kSieveThreads, 0);
+        case 5: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                    blocks_per_sm, sieve_kernel<SETUP_PLAN, true, 2, WALK_T64, 4>, kSieveThreads, 0);
+        case 6: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                    blocks_per_sm, sieve_kernel<SETUP_PLAN, true, 3, WALK_T64, 4>, kSieveThreads, 0);
+        default: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                    blocks_per_sm, sieve_kernel<SETUP_PLAN, true, 3, WALK_ANY, 2>, kSieveThreads, 0);
     }
 }
 

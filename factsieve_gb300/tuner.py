@@ -1,13 +1,15 @@
 """Autotuner for the sieve launch shape.
 
 Knobs (fs_tuning in include/factsieve.h):
-  sieve_variant         the sieve kernel built for 2, 3 or 4 resident 256-thread
-                        blocks per SM (a register cap of 128, 85 or 64)
-  sieve_blocks_per_sm   persistent blocks launched per SM
+  sieve_variant         the sieve kernel build: 3 = two candidates per thread
+                        at 3 resident 256-thread blocks per SM (register cap
+                        85), 5 / 6 = four candidates per thread (two
+                        interleaved pairs) at 2 / 3 blocks per SM
+  sieve_blocks_per_sm   blocks launched per SM (beyond the resident ones they
+                        run as later waves, which evens out the last wave)
   segment width         p-width of one launch (candidates per launch: larger
                         segments shorten the partial last wave)
-Primes per thread (2, interleaved in the walk) and the block size (256) are
-fixed in the kernels.
+The block size (256) is fixed in the kernels.
 
 A configuration is timed on a short sample of the real workload with CUDA
 events (fs_get_stats), the fastest wins, and the choice is cached in a JSON
@@ -60,12 +62,15 @@ class TuningCache:
             os.replace(tmp, self.path)
 
 
-def candidates(occupancy_by_variant):
-    """Configurations to try: every variant at its occupancy, and at 2x blocks."""
+VARIANTS = (3, 5, 6)
+
+
+def candidates(default_blocks_by_variant):
+    """Configurations to try: every variant at its default blocks per SM, and at 2x."""
     out = []
-    for v, occ in occupancy_by_variant.items():
-        out.append({"sieve_variant": v, "sieve_blocks_per_sm": occ})
-        out.append({"sieve_variant": v, "sieve_blocks_per_sm": 2 * occ})
+    for v, d in default_blocks_by_variant.items():
+        out.append({"sieve_variant": v, "sieve_blocks_per_sm": d})
+        out.append({"sieve_variant": v, "sieve_blocks_per_sm": 2 * d})
     return out
 
 
@@ -96,7 +101,7 @@ def autotune(ctx, pmin, nmin, nmax, gpu_name="gpu", sample_steps=2e10, cache: Tu
         if hit:
             return hit
     occ = {}
-    for v in (2, 3, 4):
+    for v in VARIANTS:
         ctx.set_tuning(sieve_variant=v)
         occ[v] = ctx.tuning()["sieve_blocks_per_sm"]
     per_cand = (nmax - nmin) + 0.1 * nmin + 64

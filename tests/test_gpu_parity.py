@@ -203,6 +203,8 @@ def test_hit_overflow_is_reported(ctx):
     ((1 << 36) + 1, (1 << 36) + 300_000, 500_000, 500_300),        # lazy 64-bit step, large multipliers
     ((1 << 33) - 150_000, (1 << 33) + 150_000, 2000, 2900),         # generic / lazy boundary at 2^33
     (8 * 10**12, 8 * 10**12 + 300_000, 524_000, 524_400),          # multipliers across 2^19
+    ((1 << 36) - 150_000, (1 << 36) + 150_000, 2000, 2900),         # lazy / half-offset boundary at p = 2^36
+    ((1 << 40) - 150_000, (1 << 40) + 150_000, 1_047_700, 1 << 20),    # half-offset limit p kmax = 2^60
 ])
 def test_walk_regimes_match_oracle(ctx, orc, lo, hi, nmin, nmax):
     """Every walk regime (and a pair straddling two) gives the oracle's residues, sums and hits."""
@@ -253,3 +255,67 @@ def test_search_matches_long_fixture(ctx, name):
     r = ctx.sieve(g["pmin"], g["pmax"], g["nmin"], g["nmax"], threads=16)
     assert (r.primecount, f"{r.raw_sum:016X}", f"{r.checksum:016X}", r.factorcount) == \
         (g["primecount"], g["raw_sum"], g["checksum"], g["factorcount"])
+
+
+@pytest.mark.parametrize("variant", [5, 6])
+@pytest.mark.parametrize("case", [2, 4, 5])
+def test_four_candidate_kernel_reference_selftests(ctx, variant, case):
+    """The four-candidates-per-thread sieve (two interleaved pairs) on the reference's
+    self tests: lazy 64-bit walk (case 2) and lazy 96-bit walk (cases 4, 5), each
+    with true factors, so the pair-wise hit replay runs."""
+    pmin, pmax, nmin, nmax, fc, pc, cs = SELFTEST[case]
+    try:
+        ctx.set_tuning(sieve_variant=variant)
+        r = ctx.sieve(pmin, pmax, nmin, nmax, threads=16)
+    finally:
+        ctx.set_tuning()
+    assert (r.factorcount, r.primecount, r.checksum) == (fc, pc, cs)
+
+
+@pytest.mark.parametrize("variant", [5, 6])
+@pytest.mark.parametrize("lo,hi,nmin,nmax", [
+    ((1 << 63) + 1, (1 << 63) + 300_001, 5_000, 5_700),             # canonical 96-bit walk
+    ((1 << 64) - 400_000, (1 << 64) - 1, 1_000, 1_333),              # canonical 96-bit walk near 2^64
+    (4 * 10**12, 4 * 10**12 + 200_000, 1_000_000, 1_000_300),      # mixed steps: pairs one after the other
+    (10**12 + 7, 10**12 + 300_007, 100_000, 100_701),               # lazy 64-bit, odd n-range (tail steps)
+    ((1 << 33) - 150_000, (1 << 33) + 150_000, 2000, 2900),         # generic / lazy boundary
+])
+def test_four_candidate_kernel_matches_oracle(ctx, orc, variant, lo, hi, nmin, nmax):
+    want = orc.run(lo, hi, nmin, nmax)
+    try:
+        ctx.set_tuning(sieve_variant=variant)
+        r = ctx.sieve(lo, hi, nmin, nmax, seg_width=77_777)       # many segments: ragged candidate counts
+    finally:
+        ctx.set_tuning()
+    assert (r.primecount, r.raw_sum, r.checksum, r.factorcount) == \
+        (want["primecount"], want["raw_sum"], want["checksum"], want["factorcount"])
+    assert r.lines() == [f"{int(p)} | {abs(int(nc))}!{'+1' if nc > 0 else '-1'}"
+                         for p, nc in zip(want["factors"]["p"], want["factors"]["nc"])]
+
+
+# Prime factors p >= 2^36 of n! + c for small n (found by factoring n! +- 1;
+# each is re-checked below with an exact factorial): real hits for the
+# lazy walks, including the half-offset form (p >= 2^36, p kmax <= 2^60).
+KNOWN_FACTORS = [(87178291199, 14, -1), (256443711677, 17, -1), (1713311273363831, 19, 1),
+                 (117876683047, 20, 1), (19499250680671, 20, -1), (2703875815783, 21, 1),
+                 (4826713612027, 21, -1), (93799610095769647, 22, 1), (170006681813, 22, -1),
+                 (148139754736864591, 23, 1), (498390560021687969, 23, -1), (625793187653, 24, -1),
+                 (991459181683, 24, -1), (1042190196053, 28, -1), (2778942057555023489, 29, 1),
+                 (594278556271609021, 29, -1)]
+
+
+@pytest.mark.parametrize("variant", [3, 5])
+@pytest.mark.parametrize("p,n,c", KNOWN_FACTORS)
+def test_known_large_factors_are_found(ctx, orc, variant, p, n, c):
+    import math
+    assert (math.factorial(n) + c) % p == 0
+    lo, hi, nmin, nmax = p - 3000, p + 3001, 10, 61
+    want = orc.exact_small(lo, hi, nmin, nmax)
+    assert (p, -n if c < 0 else n) in want["factors"]
+    try:
+        ctx.set_tuning(sieve_variant=variant)
+        r = ctx.sieve(lo, hi, nmin, nmax)
+    finally:
+        ctx.set_tuning()
+    assert (r.primecount, r.raw_sum, r.checksum) == (want["primecount"], want["raw_sum"], want["checksum"])
+    assert [(int(q), int(nc)) for q, nc in zip(r.factors["p"], r.factors["nc"])] == want["factors"]

@@ -16,7 +16,7 @@ class FakeCtx:
 
     def tuning(self):
         v = self.t.get("sieve_variant", 3)
-        return {"sieve_variant": v, "sieve_blocks_per_sm": {2: 2, 3: 3, 4: 4}[v]}
+        return {"sieve_variant": v, "sieve_blocks_per_sm": {3: 3, 5: 8, 6: 12}[v]}
 
 
 def test_autotune_picks_fastest_and_caches(tmp_path):
@@ -25,14 +25,14 @@ def test_autotune_picks_fastest_and_caches(tmp_path):
 
     def timer(ctx, cfg, pmin, width, nmin, nmax):
         calls.append(cfg)
-        return 100.0 * cfg["sieve_variant"] - cfg["sieve_blocks_per_sm"]   # best: variant 4 at 4 blocks
+        return 100.0 * cfg["sieve_variant"] - cfg["sieve_blocks_per_sm"]   # best: variant 6 at 12 blocks
 
     ctx = FakeCtx()
     best = tuner.autotune(ctx, 10**12, 100_000, 200_000, gpu_name="X", cache=cache, timer=timer)
-    assert (best["sieve_variant"], best["sieve_blocks_per_sm"]) == (4, 4)
+    assert (best["sieve_variant"], best["sieve_blocks_per_sm"]) == (6, 12)
     assert len(calls) == 6
     again = tuner.autotune(ctx, 10**12 + 5, 100_001, 200_003, gpu_name="X", cache=cache, timer=timer)
-    assert len(calls) == 6 and again["sieve_variant"] == 4          # same bucket: cached
+    assert len(calls) == 6 and again["sieve_variant"] == 6          # same bucket: cached
     tuner.autotune(ctx, 10**15, 100_000, 200_000, gpu_name="X", cache=cache, timer=timer)
     assert len(calls) == 12                                           # new p bucket: tuned again
 
