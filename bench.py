@@ -7,7 +7,7 @@ Workload (default config2, the plain large sieve): p in [1e12, 1e12 + 1e9),
 n in [1e5, 2e5).  One step = one p-segment of 1e8 (so 10 steps cover the
 configuration once), run through getsegprimes -> setup -> iterate -> check.
 Metric: (p,n) pair-steps/s = candidates x (nmax - nmin) / time, plus the
-fraction of the IMAD-limited Montgomery-product roofline.
+fraction of the integer-multiply roofline.
 
   value      device-resident: the segment loop on one stream, CUDA events
              around the K timed steps, L2 flushed (256 MiB write) between
@@ -17,8 +17,11 @@ fraction of the IMAD-limited Montgomery-product roofline.
              counters and hits copied back, CPU verification; wall clock.
   roofline   the dominant kernel (the fused setup/iterate/check sieve
              kernel) from CUDA events recorded around each of its launches on
-             its stream: reference-equivalent Montgomery products per second
-             against the measured IMAD rate / 20 IMAD per product.
+             its stream, against the time its walk steps and setup products
+             take at their measured ceilings (the same PTX blocks and
+             Montgomery product register-resident at full occupancy); the
+             reference's own accounting (20 IMAD per Montgomery product) and
+             the HBM fraction are reported beside it.
   cpu_baseline  the CPU oracle (OpenMP over all host cores, the reference's
              algorithm restated) on a bounded slice of the same workload.
 
@@ -73,6 +76,84 @@ def reference_setup_products(nmin: int) -> int:
         if e > 1:
             prod += (e.bit_length() - 1) + (bin(e).count("1") - 1)
     return prod
+
+
+# Ceiling microkernels (fs_bench_int_pipe kinds) of each residue step.
+STEP_CEILING_KIND = {4: (5, "half-offset lazy 64-bit step"), 1: (6, "lazy 64-bit step"),
+                     2: (7, "lazy 96-bit step"), 3: (8, "canonical 96-bit step"),
+                     0: (9, "generic Montgomery step")}
+
+
+def setup_products(fs, nmin: int) -> int:
+    """Montgomery products per candidate outside the walk: the bit-layered plan
+    (one per word, one squaring per layer after the first), the R^(D+1)
+    correction (square-and-multiply over the deficit D), the constants R mod p
+    and R^2 mod p (five squarings, built twice for four-candidate threads),
+    entering and leaving the walk's residue form and the final nmax check."""
+    words, layers, deficit = fs.setup_plan(nmin)
+    pow_d = max(int(deficit).bit_length() - 1, 0) + bin(int(deficit)).count("1")
+    return len(words) + max(len(layers) - 1, 0) + pow_d + 1 + 10 + 2 + 3
+
+
+def roofline(ctx, fs, wl, ncand, st, step_ms):
+    """Roofline of the fused sieve kernel.  The work is 64-bit modular
+    multiplication: integer multiply-add, no memory traffic to speak of (the
+    candidate list is read once).  The ceiling is the same arithmetic run
+    register-resident at full occupancy on this GPU (fs_bench_int_pipe kinds
+    4-9: the walk's own PTX step blocks and the Montgomery product), so
+    peak = pair-steps the kernel would finish if its walk ran at the walk
+    ceiling and its setup at the Montgomery-product ceiling."""
+    pmin, pmax, nmin, nmax, seg = WORKLOADS[wl]
+    W = nmax - nmin
+    step = fs.walk_step(pmin, pmin + seg, nmax)
+    kind, step_name = STEP_CEILING_KIND[step]
+    walk_ceil, _ = ctx.bench_int_pipe(kind, 4000)
+    mm_ceil, _ = ctx.bench_int_pipe(4, 4000)
+    imad_ops, _ = ctx.bench_int_pipe(0, 20000)
+    smp = setup_products(fs, nmin)
+    sieve_s = st["sieve_ms"] * 1e-3
+    launches = max(st["sieve_launches"], 1)
+    pairs = ncand * W
+    lower_bound_s = ncand * (W / walk_ceil + smp / mm_ceil)
+    achieved = pairs / sieve_s if sieve_s > 0 else 0.0
+    peak = pairs / lower_bound_s if lower_bound_s > 0 else 0.0
+    cap = NCU_CAPTURE.get(wl, {})
+    alg_bytes = 8.0 * ncand / launches                  # the candidate list, read once
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            peaks = json.load(fh)
+    except (OSError, ValueError):
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    hbm_ach = alg_bytes / (sieve_s / launches) / 1e9 if sieve_s > 0 else 0.0
+    # the reference's own accounting (a 20-IMAD Montgomery product per step and
+    # per setup product): reference-equivalent products against IMAD rate / 20
+    ref_products = ncand * (W + reference_setup_products(nmin) + 1)
+    ref_peak = imad_ops / IMAD_PER_PRODUCT
+    return {
+        "bound": "imad", "achieved": achieved / 1e9, "peak": peak / 1e9, "unit": "G pair-steps/s",
+        "frac": achieved / peak if peak else None,
+        "traffic": cap.get("traffic"), "algorithmic_bytes_per_launch": alg_bytes,
+        "kernel": "sieve_kernel (setup + walk + check fused)",
+        "kernel_ms_per_launch": st["sieve_ms"] / launches,
+        "share_of_step": st["sieve_ms"] / step_ms if step_ms else None,
+        "walk_step": step_name,
+        "ceilings": {"walk_steps_per_s": walk_ceil, "montgomery_products_per_s": mm_ceil,
+                     "imad_lane_ops_per_s": imad_ops},
+        "setup_products_per_candidate": smp,
+        "peak_source": "measured on this GPU: the walk step's PTX block and mont_mul, register-resident at full "
+                       "occupancy (fs_bench_int_pipe kinds 4-9)",
+        "imad_pipe_busy_ncu": cap.get("imad_pipe_busy"), "ncu_source": cap.get("source"),
+        "hbm": {"achieved": hbm_ach, "peak": hbm_peak, "unit": "GB/s",
+                "frac": hbm_ach / hbm_peak if hbm_peak else None,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6.8 TB/s"},
+        "reference_mulmod_roofline": {"achieved": ref_products / sieve_s / 1e9 if sieve_s > 0 else 0.0,
+                                      "peak": ref_peak / 1e9, "unit": "G Montgomery products/s",
+                                      "frac": (ref_products / sieve_s) / ref_peak if sieve_s > 0 else None,
+                                      "definition": "reference-equivalent products (one per (p,n) step plus "
+                                                    "the reference setup's products) / (IMAD rate / 20)"},
+    }
 
 
 class ClockSampler:
@@ -274,24 +355,8 @@ def run_ours(args):
     value = pairs / (ms * 1e-3)
 
     # roofline of the dominant kernel, from this rank's events
-    setup_prod = reference_setup_products(nmin)
     my_pc = primecount if not dist else int(t[4].item())
-    products = my_pc * (W + setup_prod + 1)
-    sieve_s = st["sieve_ms"] * 1e-3
-    achieved = products / sieve_s / 1e9 if sieve_s > 0 else 0.0
-    imad_ops, _ = ctx.bench_int_pipe(0, 20000)
-    peak = imad_ops / IMAD_PER_PRODUCT / 1e9
-    cap = NCU_CAPTURE.get(wl, {})
-    roof = {"bound": "imad", "achieved": achieved, "peak": peak, "unit": "Gmulmod/s",
-            "frac": achieved / peak if peak else None, "traffic": cap.get("traffic"),
-            "imad_pipe_busy_ncu": cap.get("imad_pipe_busy"), "ncu_source": cap.get("source"),
-            "algorithmic_bytes_per_launch": 8 * my_pc / max(st["sieve_launches"], 1),
-            "kernel": "sieve_kernel (setup+iterate+check, fused)",
-            "kernel_ms_per_launch": st["sieve_ms"] / max(st["sieve_launches"], 1),
-            "products_per_launch": products / max(st["sieve_launches"], 1),
-            "peak_source": "measured IMAD stream on this GPU (fs_bench_int_pipe) / 20 IMAD per "
-                           "reference Montgomery product",
-            "share_of_step": (st["sieve_ms"] + 0.0) / ms if ms else None}
+    roof = roofline(ctx, fs, wl, my_pc, st, ms)
 
     # e2e through the public API with host buffers, on rank 0's first segments
     e2e = None

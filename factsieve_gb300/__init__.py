@@ -102,6 +102,7 @@ def _declare(L):
         "fs_table_check": (C.c_int, [vp, vp, vp, u32, P64]),
         "fs_plan_check": (C.c_int, [vp, vp, vp, u32, vp, vp, u32, u64, P64]),
         "fs_bench_int_pipe": (C.c_int, [vp, u32, u32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+        "fs_walk_step": (C.c_int, [u64, u64, u32]),
         "fs_set_timing": (C.c_int, [vp, C.c_int]),
         "fs_get_stats": (C.c_int, [vp, C.POINTER(Stats)]),
         "fs_reset_stats": (C.c_int, [vp]),
@@ -190,6 +191,13 @@ def setup_plan_chunks(n: int, chunks: int):
     if rc:
         raise FSError(rc, "fs_setup_plan_chunks")
     return b, d
+
+
+def walk_step(plo: int, phi: int, kmax: int) -> int:
+    """The residue step the sieve runs for p in [plo, phi), multipliers up to kmax
+    (4 half-offset lazy 64-bit, 1 lazy 64-bit, 2 lazy 96-bit, 3 canonical 96-bit,
+    0 chosen per candidate)."""
+    return int(lib().fs_walk_step(plo, phi, kmax))
 
 
 def find_wheel_offset(start: int):

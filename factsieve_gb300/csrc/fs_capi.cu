@@ -736,8 +736,10 @@ int fs_plan_check(fs_ctx* c, const uint64_t* d_cand, fs_counters* d_ctr, uint32_
     return FS_OK;
 }
 
+int fs_walk_step(uint64_t plo, uint64_t phi, uint32_t kmax) { return fs::walk_for_range(plo, phi, kmax); }
+
 int fs_bench_int_pipe(fs_ctx* c, uint32_t kind, uint32_t iters, double* ops_per_sec, double* ms) {
-    if (!c || kind > 3) return FS_E_ARG;
+    if (!c || kind > 9 || iters == 0 || iters > (1u << 24)) return FS_E_ARG;
     int rc = bind(c);
     if (rc) return rc;
     const int grid = c->sm_count * 8;   // 8 x 256 threads = 2048 per SM
@@ -753,7 +755,7 @@ int fs_bench_int_pipe(fs_ctx* c, uint32_t kind, uint32_t iters, double* ops_per_
     CK(c, cudaEventElapsedTime(&t, e0, e1));
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    const double ops = (double)grid * 256.0 * (double)iters * 8.0;
+    const double ops = (double)grid * 256.0 * (double)iters * fs::bench_units_per_thread_iter(kind);
     if (ms) *ms = t;
     if (ops_per_sec) *ops_per_sec = t > 0 ? ops / (t * 1e-3) : 0;
     return FS_OK;

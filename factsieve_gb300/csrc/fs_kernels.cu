@@ -1007,6 +1007,107 @@ __global__ void __launch_bounds__(256) imad_bench_kernel(u32 iters, u32 kind, u3
     if (x == seed) sink[blockIdx.x] = x;   // practically never true, but not provable
 }
 
+// ======================================================= ceilings ====
+//
+// The sieve's own arithmetic with nothing else: register-resident chains at
+// full occupancy, no loads, no stores but one guarded word.  Their rates
+// are the speed of light of that instruction mix on this GPU, the
+// denominator of the sieve kernel's roofline.
+//   kind 4  Montgomery products (mont_mul), 8 chains per thread
+//   kind 5  half-offset lazy steps (the half_walk8x2 block), 4 chains
+//   kind 6  lazy 64-bit steps (lazy_walk8x2), 4 chains
+//   kind 7  lazy 96-bit steps (lazy96_walk8x2), 4 chains
+//   kind 8  canonical 96-bit steps (canon96_walk8x2), 4 chains
+//   kind 9  generic Montgomery steps (mont_mul by kR, k advanced by R), 4 chains
+constexpr u32 kCeilUnits[10] = {0, 0, 0, 0, 8, 32, 32, 32, 32, 4};
+
+template <u32 kind>
+__global__ void __launch_bounds__(256) ceiling_kernel(u32 iters, u32 seed, u32* sink) {
+    const u32 tid = blockIdx.x * blockDim.x + threadIdx.x;
+    // moduli in each regime's range (odd; the arithmetic is exact for any odd modulus)
+    u64 base;
+    switch (kind) {
+        case 5: base = 1000000000000ull; break;           // p kmax <= 2^60
+        case 6: base = (1ull << 34) + 1; break;           // 2^33 < p, p kmax <= 2^62
+        case 7: base = 1000000000000000ull; break;        // p kmax > 2^62, p < 2^63
+        case 8: base = (1ull << 63) + 1; break;           // p >= 2^63
+        default: base = (1ull << 63) + 1; break;
+    }
+    Prime c[4];
+#pragma unroll
+    for (int h = 0; h < 4; ++h) c[h] = make_prime((base + 2ull * (4ull * tid + h) + 2ull * seed) | 1ull);
+    const u32 k0 = 100001;   // multipliers k0 .. k0 + 8 iters: below 2^28 and p k below each regime's bound
+    u32 acc = 0;
+    if constexpr (kind == 4) {
+        u64 x[8];
+#pragma unroll
+        for (int h = 0; h < 8; ++h) x[h] = c[h & 3].one + h;
+        const u64 y = c[0].r2;
+        for (u32 it = 0; it < iters; ++it) {
+#pragma unroll
+            for (int h = 0; h < 8; ++h) x[h] = mont_mul(x[h], y, c[h & 3].p, c[h & 3].pinv);
+        }
+#pragma unroll
+        for (int h = 0; h < 8; ++h) acc ^= (u32)x[h] ^ (u32)(x[h] >> 32);
+    } else if constexpr (kind == 9) {
+        u64 r[4], k[4];
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+            r[h] = c[h].one;
+            k[h] = to_mont(k0, c[h]);
+        }
+        for (u32 it = 0; it < iters; ++it) {
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {
+                acc += (r[h] == c[h].one) | (r[h] == c[h].p - c[h].one);
+                r[h] = mont_mul(r[h], k[h], c[h].p, c[h].pinv);
+                k[h] = mod_add(k[h], c[h].one, c[h].p);
+            }
+        }
+#pragma unroll
+        for (int h = 0; h < 4; ++h) acc ^= (u32)r[h];
+    } else {
+        u32 l[4], hh[4];
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+            l[h] = (u32)c[h].one;
+            hh[h] = (u32)(c[h].one >> 32);
+        }
+        if constexpr (kind == 5) {
+            const Half64 A = make_half(c[0]), B = make_half(c[1]), C = make_half(c[2]), D = make_half(c[3]);
+            for (u32 it = 0; it < iters; ++it) {
+                acc += half_walk8x2(l[0], hh[0], l[1], hh[1], k0 + 8 * it, A, B);
+                acc += half_walk8x2(l[2], hh[2], l[3], hh[3], k0 + 8 * it, C, D);
+            }
+        } else if constexpr (kind == 6) {
+            const Lazy64 A = make_lazy(c[0]), B = make_lazy(c[1]), C = make_lazy(c[2]), D = make_lazy(c[3]);
+            for (u32 it = 0; it < iters; ++it) {
+                acc += lazy_walk8x2(l[0], hh[0], l[1], hh[1], k0 + 8 * it, A, B);
+                acc += lazy_walk8x2(l[2], hh[2], l[3], hh[3], k0 + 8 * it, C, D);
+            }
+        } else if constexpr (kind == 7) {
+            const u32 kmax = k0 + 8 * iters;
+            const Lazy96 A = make_lazy96(c[0], kmax), B = make_lazy96(c[1], kmax);
+            const Lazy96 C = make_lazy96(c[2], kmax), D = make_lazy96(c[3], kmax);
+            for (u32 it = 0; it < iters; ++it) {
+                acc += lazy96_walk8x2(l[0], hh[0], l[1], hh[1], k0 + 8 * it, A, B);
+                acc += lazy96_walk8x2(l[2], hh[2], l[3], hh[3], k0 + 8 * it, C, D);
+            }
+        } else {
+            const u32 kmax = k0 + 8 * iters;
+            const Canon96 A = make_canon96(c[0], kmax), B = make_canon96(c[1], kmax);
+            const Canon96 C = make_canon96(c[2], kmax), D = make_canon96(c[3], kmax);
+            for (u32 it = 0; it < iters; ++it) {
+                acc += canon96_walk8x2(l[0], hh[0], l[1], hh[1], k0 + 8 * it, A, B);
+                acc += canon96_walk8x2(l[2], hh[2], l[3], hh[3], k0 + 8 * it, C, D);
+            }
+        }
+#pragma unroll
+        for (int h = 0; h < 4; ++h) acc ^= l[h] ^ hh[h];
+    }
+    if (acc == 0x9E3779B9u) sink[blockIdx.x & 4095] = acc;   // keeps the work; practically never stores
+}
+
 // ============================================================== launches ===
 
 cudaError_t launch_gen(const GenArgs& a, int grid, cudaStream_t s) {
@@ -1097,9 +1198,19 @@ cudaError_t launch_table_check(const TableCheckArgs& a, int grid, cudaStream_t s
 }
 
 cudaError_t launch_imad_bench(u32 iters, u32 kind, u32 seed, u32* sink, int grid, cudaStream_t s) {
-    imad_bench_kernel<<<grid, 256, 0, s>>>(iters, kind, seed, sink);
+    switch (kind) {
+        case 4: ceiling_kernel<4><<<grid, 256, 0, s>>>(iters, seed, sink); break;
+        case 5: ceiling_kernel<5><<<grid, 256, 0, s>>>(iters, seed, sink); break;
+        case 6: ceiling_kernel<6><<<grid, 256, 0, s>>>(iters, seed, sink); break;
+        case 7: ceiling_kernel<7><<<grid, 256, 0, s>>>(iters, seed, sink); break;
+        case 8: ceiling_kernel<8><<<grid, 256, 0, s>>>(iters, seed, sink); break;
+        case 9: ceiling_kernel<9><<<grid, 256, 0, s>>>(iters, seed, sink); break;
+        default: imad_bench_kernel<<<grid, 256, 0, s>>>(iters, kind, seed, sink); break;
+    }
     return cudaGetLastError();
 }
+
+double bench_units_per_thread_iter(u32 kind) { return kind < 4 ? 8.0 : (kind < 10 ? kCeilUnits[kind] : 0.0); }
 
 int walk_for_range(uint64_t plo, uint64_t phi, uint32_t kmax) {
     if (phi <= plo || kmax == 0) return WALK_ANY;

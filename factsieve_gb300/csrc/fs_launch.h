@@ -125,6 +125,7 @@ int walk_for_range(uint64_t plo, uint64_t phi, uint32_t kmax);
 cudaError_t launch_setup_partial(const SieveArgs& a, int grid_x, int nchunks, cudaStream_t s);
 cudaError_t launch_table_check(const TableCheckArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_imad_bench(u32 iters, u32 kind, u32 seed, u32* sink, int grid, cudaStream_t s);
+double bench_units_per_thread_iter(u32 kind);
 cudaError_t sieve_occupancy(int* blocks_per_sm, int variant);
 int sieve_threads();
 int gen_threads();
