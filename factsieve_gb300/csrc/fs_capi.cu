@@ -929,7 +929,7 @@ extern "C" int fs_batch_prepare(fs_ctx* c, const fs_job* jobs, uint32_t njobs, u
         dj[k].nend = j.nmax;
         dj[k].layer_begin = layer_range[j.nmin].first;
         dj[k].layer_end = layer_range[j.nmin].second;
-        dj[k].pad = 0;
+        dj[k].walk = (u32)fs::walk_for_range(j.pmin, j.pmax, j.nmax);
         dj[k].deficit = deficit[j.nmin];
     }
     CK(c, cudaMemcpy(b.d_words, words.data(), words.size() * sizeof(u64), cudaMemcpyHostToDevice));

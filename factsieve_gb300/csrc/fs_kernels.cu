@@ -522,6 +522,38 @@ __device__ __forceinline__ void walk_quad_as(u64 (&r)[4], Prime (&c)[4], u32 nre
     }
 }
 
+// The same with the step chosen at run time (one job's code, uniform over a
+// block's tile).
+__device__ __forceinline__ void walk_quad_rt(int walk, u64 (&r)[4], Prime (&c)[4], u32 nreal, u32 nstart, u32 nend,
+                                             const WalkOut& o) {
+    switch (walk) {
+        case WALK_H64: walk_quad_as<WALK_H64>(r, c, nreal, nstart, nend, o); break;
+        case WALK_T64: walk_quad_as<WALK_T64>(r, c, nreal, nstart, nend, o); break;
+        case WALK_L96: walk_quad_as<WALK_L96>(r, c, nreal, nstart, nend, o); break;
+        case WALK_C96: walk_quad_as<WALK_C96>(r, c, nreal, nstart, nend, o); break;
+        default: walk_quad_as<WALK_ANY>(r, c, nreal, nstart, nend, o); break;
+    }
+}
+
+// The last three of four candidates of a thread, duplicates of the first
+// where the list ends.
+__device__ __forceinline__ u32 load_quad(const u64* cand, u32 i0, u32 n, Prime (&c)[4]) {
+    const u32 nreal = n - i0 < 4 ? n - i0 : 4;
+    c[0] = make_prime(cand[i0]);
+#pragma unroll
+    for (int h = 1; h < 4; ++h) c[h] = (u32)h < nreal ? make_prime(cand[i0 + h]) : c[0];
+    return nreal;
+}
+
+// s6 + s7 of one finished candidate and its nmax round trip (check.cl:50-109).
+__device__ __forceinline__ void final_check(const Prime& c, u64 r, u32 nmax, u64& sum, u32& bad) {
+    const u64 s7 = to_mont(nmax, c);
+    u32 back = (u32)mont_mul(s7, 1, c.p, c.pinv);
+    if (c.p <= nmax && nmax % c.p == back) back = nmax;
+    bad += back != nmax;
+    sum += r + s7;
+}
+
 // Starting residue of candidate i (SETUP mode), before the walk.
 template <int SETUP>
 __device__ __forceinline__ u64 start_residue_one(const SieveArgs& a, const Prime& c, u32 i) {
@@ -689,19 +721,21 @@ __global__ void __launch_bounds__(kSieveThreads) setup_partial_kernel(SieveArgs 
 
 // ============================================================ batches ====
 
-// Persistent kernel over many uneven jobs.  A tile is 2 x blockDim candidates
-// of one job; blocks take tiles from a global counter until the batch is
-// done.  The host orders jobs by estimated work per candidate, heaviest
-// first, so the long tiles start early and the tail is made of short ones.
+// Persistent kernel over many uneven jobs.  A tile is kTileCandidates
+// candidates of one job, four per thread; blocks take tiles from a global
+// counter until the batch is done.  The host orders jobs by estimated work
+// per candidate, heaviest first, so the long tiles start early and the tail
+// is made of short ones.  Each job carries the walk step valid for its whole
+// p-range, uniform over a tile.
 constexpr int kBatchMaxJobs = 1024;
 
-__global__ void __launch_bounds__(kSieveThreads, 3) batch_sieve_kernel(BatchArgs a) {
+__global__ void __launch_bounds__(kSieveThreads, 2) batch_sieve_kernel(BatchArgs a) {
     __shared__ HitStage st;
     __shared__ u32 tile_end[kBatchMaxJobs];   // inclusive prefix sum of tiles per job
     __shared__ u32 s_tile;
     __shared__ u64 wsum[kSieveThreads / 32];
     __shared__ u32 wbad[kSieveThreads / 32];
-    const u32 per_tile = 2 * blockDim.x;
+    const u32 per_tile = kTileCandidates;
     if (threadIdx.x == 0) {
         st.n = 0;
         u32 acc = 0;
@@ -731,30 +765,21 @@ __global__ void __launch_bounds__(kSieveThreads, 3) batch_sieve_kernel(BatchArgs
         const BatchJob& J = a.jobs[j];
         const u32 nc = a.ctr[j].ncand;
         const u32 n = nc < J.cap ? nc : J.cap;
-        const u32 first = (t - (j ? tile_end[j - 1] : 0)) * per_tile;
-        const u32 ia = first + 2 * threadIdx.x, ib = ia + 1;
+        const u32 i0 = (t - (j ? tile_end[j - 1] : 0)) * per_tile + 4 * threadIdx.x;
         u64 sum = 0;
         u32 bad = 0;
-        if (ia < n) {
+        if (i0 < n) {
             const WalkOut o{&st, a.hits, a.hitcap, a.gctr, (int)j};
-            const bool real_b = ib < n;
-            const Prime ca = make_prime(J.cand[ia]);
-            const Prime cb = real_b ? make_prime(J.cand[ib]) : ca;
-            u64 ra, rb;
-            plan_product2(ca, cb, a.words, a.layers, J.layer_begin, J.layer_end, ra, rb);
-            ra = mont_mul(ra, mont_pow(ca.r2, J.deficit, ca), ca.p, ca.pinv);
-            rb = mont_mul(rb, mont_pow(cb.r2, J.deficit, cb), cb.p, cb.pinv);
-            walk_pair(ra, rb, ca, cb, real_b, J.nstart, J.nend, o);
+            Prime c[4];
+            const u32 nreal = load_quad(J.cand, i0, n, c);
+            u64 r[4];
+            plan_product4(c, a.words, a.layers, J.layer_begin, J.layer_end, r);
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                if (h == 1 && !real_b) break;
-                const Prime& c = h ? cb : ca;
-                const u64 s7 = to_mont(J.nend, c);
-                u32 back = (u32)mont_mul(s7, 1, c.p, c.pinv);
-                if (c.p <= J.nend && J.nend % c.p == back) back = J.nend;
-                bad += back != J.nend;
-                sum += (h ? rb : ra) + s7;
-            }
+            for (int h = 0; h < 4; ++h) r[h] = mont_mul(r[h], mont_pow(c[h].r2, J.deficit, c[h]), c[h].p, c[h].pinv);
+            walk_quad_rt((int)J.walk, r, c, nreal, J.nstart, J.nend, o);
+#pragma unroll
+            for (int h = 0; h < 4; ++h)
+                if ((u32)h < nreal) final_check(c[h], r[h], J.nend, sum, bad);
         }
 #pragma unroll
         for (int d = 16; d; d >>= 1) {
@@ -795,19 +820,19 @@ __global__ void __launch_bounds__(kSieveThreads, 3) batch_sieve_kernel(BatchArgs
 
 // ============================================================ serving ====
 
-// One round of the serving loop: a list of tiles, each up to 2 x blockDim
+// One round of the serving loop: a list of tiles, each up to kTileCandidates
 // candidates of one job in one phase (starting residue from the plan, a
-// chunk of the walk, the final checksum), taken from a global counter by
-// persistent blocks.  Residues live in each job's device buffer between
-// rounds.
-__global__ void __launch_bounds__(kSieveThreads, 3) serve_round_kernel(ServeArgs a) {
+// chunk of the walk, the final checksum), four per thread, taken from a
+// global counter by persistent blocks.  Residues live in each job's device
+// buffer between rounds.
+__global__ void __launch_bounds__(kSieveThreads, 2) serve_round_kernel(ServeArgs a) {
     __shared__ HitStage st;
     __shared__ u32 s_tile;
     __shared__ u64 wsum[kSieveThreads / 32];
     __shared__ u32 wbad[kSieveThreads / 32];
     if (threadIdx.x == 0) st.n = 0;
     __syncthreads();
-    const u32 per_tile = 2 * blockDim.x;
+    const u32 per_tile = kTileCandidates;
     const u32 ntiles = a.nchunks ? a.chunks[a.nchunks - 1].tile_end : 0;
     for (;;) {
         if (threadIdx.x == 0) s_tile = atomicAdd(a.tile_counter, 1u);
@@ -824,43 +849,37 @@ __global__ void __launch_bounds__(kSieveThreads, 3) serve_round_kernel(ServeArgs
         }
         const ServeChunk T = a.chunks[lo];
         const u32 tile0 = lo ? a.chunks[lo - 1].tile_end : 0;
-        const u32 first = T.first + (t - tile0) * per_tile;
-        const u32 ia = first + 2 * threadIdx.x, ib = ia + 1;
+        const u32 i0 = T.first + (t - tile0) * per_tile + 4 * threadIdx.x;
         const u32 end = T.first + T.count;
         u64 sum = 0;
         u32 bad = 0;
-        if (ia < end) {
+        if (i0 < end) {
             const WalkOut o{&st, a.hits, a.hitcap, a.gctr, (int)T.tag};
-            const bool real_b = ib < end;
-            const Prime ca = make_prime(T.cand[ia]);
-            const Prime cb = real_b ? make_prime(T.cand[ib]) : ca;
-            u64 ra, rb;
+            Prime c[4];
+            const u32 nreal = load_quad(T.cand, i0, end, c);
+            u64 r[4];
             if (T.flags & SERVE_SETUP) {
-                plan_product2(ca, cb, T.words, T.layers, T.layer_begin, T.layer_end, ra, rb);
-                ra = mont_mul(ra, mont_pow(ca.r2, T.deficit, ca), ca.p, ca.pinv);
-                rb = mont_mul(rb, mont_pow(cb.r2, T.deficit, cb), cb.p, cb.pinv);
+                plan_product4(c, T.words, T.layers, T.layer_begin, T.layer_end, r);
+#pragma unroll
+                for (int h = 0; h < 4; ++h)
+                    r[h] = mont_mul(r[h], mont_pow(c[h].r2, T.deficit, c[h]), c[h].p, c[h].pinv);
             } else {
-                ra = T.residue[ia];
-                rb = real_b ? T.residue[ib] : ra;
+                r[0] = T.residue[i0];
+#pragma unroll
+                for (int h = 1; h < 4; ++h) r[h] = (u32)h < nreal ? T.residue[i0 + h] : r[0];
             }
-            walk_pair(ra, rb, ca, cb, real_b, T.nstart, T.nend, o);
+            walk_quad_rt((int)T.walk, r, c, nreal, T.nstart, T.nend, o);
             if (T.flags & SERVE_FINAL) {
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    if (h == 1 && !real_b) break;
-                    const Prime& c = h ? cb : ca;
-                    const u64 s7 = to_mont(T.nend, c);
-                    u32 back = (u32)mont_mul(s7, 1, c.p, c.pinv);
-                    if (c.p <= T.nend && T.nend % c.p == back) back = T.nend;
-                    bad += back != T.nend;
-                    sum += (h ? rb : ra) + s7;
-                }
+                for (int h = 0; h < 4; ++h)
+                    if ((u32)h < nreal) final_check(c[h], r[h], T.nend, sum, bad);
             } else {
-                T.residue[ia] = ra;
-                if (real_b) T.residue[ib] = rb;
+#pragma unroll
+                for (int h = 0; h < 4; ++h)
+                    if ((u32)h < nreal) T.residue[i0 + h] = r[h];
             }
         }
-        if (T.flags & SERVE_FINAL) {
+    if (T.flags & SERVE_FINAL) {
 #pragma unroll
             for (int d = 16; d; d >>= 1) {
                 sum += __shfl_xor_sync(0xffffffffu, sum, d);

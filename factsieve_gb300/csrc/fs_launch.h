@@ -66,7 +66,7 @@ struct BatchJob {
     u32 cap;
     u32 nstart, nend;            // walk [nstart, nend); s7 = nend * R
     u32 layer_begin, layer_end;  // its plan's layers in the shared layer table
-    u32 pad;
+    u32 walk;                    // WALK_* step valid for the job's whole p-range
     u64 deficit;
 };
 
@@ -82,8 +82,11 @@ struct BatchArgs {
     u32 hitcap;
 };
 
+// Candidates per tile of the batch and serving kernels (four per thread).
+constexpr u32 kTileCandidates = 4 * 256;
+
 // Serving round: one chunk = a block of one job's candidates in one phase;
-// the kernel cuts chunks into tiles of 2 x 256 candidates.
+// the kernel cuts chunks into tiles of kTileCandidates.
 enum : u32 { SERVE_SETUP = 1u, SERVE_FINAL = 2u };
 struct ServeChunk {
     const u64* cand;
@@ -98,7 +101,7 @@ struct ServeChunk {
     u32 flags;                   // SERVE_SETUP: start from the plan; SERVE_FINAL: checksum, no store
     u32 tag;                     // job slot, stored in hit records
     u32 tile_end;                // inclusive prefix of tiles over the round's chunks
-    u32 pad;
+    u32 walk;                    // WALK_* step valid for the job's whole p-range and this chunk's n
 };
 
 constexpr int kServeMaxChunks = 4096;

@@ -362,7 +362,7 @@ extern "C" int fs_serve_round(fs_ctx* c, uint32_t* n_active, uint32_t* n_queued)
         if (j.state == fs_serve::SETUP) {
             const double per = 2.7 * (double)j.nwords + 64.0;
             uint64_t cnt = (uint64_t)std::max(4096.0, std::max(budget, 0.0) / per);
-            cnt = (cnt + 511) / 512 * 512;
+            cnt = (cnt + fs::kTileCandidates - 1) / fs::kTileCandidates * fs::kTileCandidates;
             ch.first = j.setup_next;
             ch.count = (uint32_t)std::min<uint64_t>(cnt, j.ncand - j.setup_next);
             ch.flags = fs::SERVE_SETUP;
@@ -395,12 +395,13 @@ extern "C" int fs_serve_round(fs_ctx* c, uint32_t* n_active, uint32_t* n_queued)
             j.walk_n = ch.nend;
             budget -= (double)j.ncand * (double)steps;
         }
+        ch.walk = (u32)fs::walk_for_range(j.spec.pmin, j.spec.pmax, ch.nend);
         hc[nch++] = ch;
         s.next_job = (slot + 1) % S;
     }
     uint32_t tiles = 0;
     for (uint32_t k = 0; k < nch; ++k) {
-        tiles += (hc[k].count + 511) / 512;
+        tiles += (hc[k].count + fs::kTileCandidates - 1) / fs::kTileCandidates;
         hc[k].tile_end = tiles;
     }
     // 2. queue the round
