@@ -95,7 +95,7 @@ def setup_products(fs, nmin: int) -> int:
     return len(words) + max(len(layers) - 1, 0) + pow_d + 1 + 10 + 2 + 3
 
 
-def roofline(ctx, fs, wl, ncand, st, step_ms):
+def roofline(ctx, fs, wl, ncand, st, step_ms, clocks=None):
     """Roofline of the fused sieve kernel.  The work is 64-bit modular
     multiplication: integer multiply-add, no memory traffic to speak of (the
     candidate list is read once).  The ceiling is the same arithmetic run
@@ -131,6 +131,8 @@ def roofline(ctx, fs, wl, ncand, st, step_ms):
     # per setup product): reference-equivalent products against IMAD rate / 20
     ref_products = ncand * (W + reference_setup_products(nmin) + 1)
     ref_peak = imad_ops / IMAD_PER_PRODUCT
+    sm = (clocks or {}).get("sm_mhz") or 0
+    sm_max = (clocks or {}).get("sm_max_mhz") or 0
     return {
         "bound": "imad", "achieved": achieved / 1e9, "peak": peak / 1e9, "unit": "G pair-steps/s",
         "frac": achieved / peak if peak else None,
@@ -148,11 +150,15 @@ def roofline(ctx, fs, wl, ncand, st, step_ms):
         "hbm": {"achieved": hbm_ach, "peak": hbm_peak, "unit": "GB/s",
                 "frac": hbm_ach / hbm_peak if hbm_peak else None,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6.8 TB/s"},
-        "reference_mulmod_roofline": {"achieved": ref_products / sieve_s / 1e9 if sieve_s > 0 else 0.0,
-                                      "peak": ref_peak / 1e9, "unit": "G Montgomery products/s",
-                                      "frac": (ref_products / sieve_s) / ref_peak if sieve_s > 0 else None,
-                                      "definition": "reference-equivalent products (one per (p,n) step plus "
-                                                    "the reference setup's products) / (IMAD rate / 20)"},
+        "reference_mulmod_roofline": {
+            "achieved": ref_products / sieve_s / 1e9 if sieve_s > 0 else 0.0,
+            "peak": ref_peak / 1e9, "unit": "G Montgomery products/s",
+            "frac": (ref_products / sieve_s) / ref_peak if sieve_s > 0 else None,
+            "iterate_only_frac": (pairs / sieve_s) / ref_peak if sieve_s > 0 else None,
+            "peak_at_max_clock": ref_peak / 1e9 * (sm_max / sm) if sm and sm_max else None,
+            "definition": "reference-equivalent products (one per (p,n) step plus the reference setup's table "
+                          "products and one check) / (measured IMAD rate / 20 IMAD per product), at the sampled "
+                          "clock; iterate_only counts the walk steps alone"},
     }
 
 
@@ -238,16 +244,24 @@ def cpu_slice_run(pmin, nmin, nmax, width):
     return r, dt
 
 
-def cpu_baseline(wl, budget_s=15.0):
+def cpu_baseline(wl, budget_s=40.0):
+    """The oracle on all host cores: config 1 in full, configs 2 and 3 on the
+    fixed contiguous 1/100 slice at the start of the p-range (the work is
+    uniform in p, so pair-steps/s carry over), shrunk only if a probe says the
+    slice would take longer than budget_s."""
     pmin, pmax, nmin, nmax, seg = WORKLOADS[wl]
-    # size the slice from a short probe so the measurement takes ~budget_s
-    probe = max(20_000, min(seg, 200_000))
+    width = pmax - pmin if wl == "config1" else (pmax - pmin) // 100
+    probe = max(20_000, min(width, 200_000))
     r, dt = cpu_slice_run(pmin, nmin, nmax, probe)
-    width = int(min(seg, max(probe, probe * budget_s / max(dt, 1e-3))))
+    est = dt * width / probe
+    label = "the whole range" if wl == "config1" else "the fixed 1/100 slice"
+    if est > budget_s:
+        width = int(max(probe, width * budget_s / est))
+        label = f"a {width}-wide slice (the 1/100 slice would take ~{est:.0f} s)"
     r, dt = cpu_slice_run(pmin, nmin, nmax, width)
     pairs = r["primecount"] * (nmax - nmin)
     return {"value": pairs / dt, "unit": "pair-steps/s", "cores": os.cpu_count(), "kind": "port",
-            "sample": f"p in [{pmin}, {pmin + width}) of the workload ({r['primecount']} candidates, "
+            "sample": f"{label}: p in [{pmin}, {pmin + width}) ({r['primecount']} candidates, "
                       f"n in [{nmin}, {nmax})), oracle/oracle.c OpenMP, {dt:.1f} s"}
 
 
@@ -356,7 +370,7 @@ def run_ours(args):
 
     # roofline of the dominant kernel, from this rank's events
     my_pc = primecount if not dist else int(t[4].item())
-    roof = roofline(ctx, fs, wl, my_pc, st, ms)
+    roof = roofline(ctx, fs, wl, my_pc, st, ms, clk.summary())
 
     # e2e through the public API with host buffers, on rank 0's first segments
     e2e = None
@@ -377,6 +391,13 @@ def run_ours(args):
         e2e = {"value": e2e_pairs / dt, "unit": "pair-steps/s", "h2d_bytes_per_step": h2d // e2e_steps,
                "d2h_bytes_per_step": d2h // e2e_steps, "steps": e2e_steps,
                "path": "Context.sieve (fs_search_begin/segment/collect + fs_postprocess)"}
+
+    if e2e:
+        # the reference accounting end to end: e2e pair-steps/s with each step's
+        # share of the reference's setup and check products
+        ref = roof["reference_mulmod_roofline"]
+        per_step = (W + reference_setup_products(nmin) + 1) / W
+        ref["end_to_end_frac"] = e2e["value"] * per_step / (ref["peak"] * 1e9) if ref["peak"] else None
 
     if rank == 0:
         cpu = cpu_baseline(wl) if (ws == 1 and not args.no_cpu) else None
