@@ -195,8 +195,8 @@ def setup_plan_chunks(n: int, chunks: int):
 
 def walk_step(plo: int, phi: int, kmax: int) -> int:
     """The residue step the sieve runs for p in [plo, phi), multipliers up to kmax
-    (4 half-offset lazy 64-bit, 1 lazy 64-bit, 2 lazy 96-bit, 3 canonical 96-bit,
-    0 chosen per candidate)."""
+    (4 / 5 half-offset lazy 64-bit / 96-bit, 1 lazy 64-bit, 2 lazy 96-bit,
+    3 canonical 96-bit, 0 chosen per candidate)."""
     return int(lib().fs_walk_step(plo, phi, kmax))
 
 

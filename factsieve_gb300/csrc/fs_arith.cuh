@@ -453,9 +453,7 @@ __device__ __forceinline__ Half64 make_half(const Prime& c) {
 
 // n! R (canonical) -> n! x, and back: x R^-1 by one Montgomery product with
 // x, and x^-1 = -2 by one with -2 R^2.
-__device__ __forceinline__ u64 half_enter(u64 r, const Prime& c, const Half64& H) {
-    return mont_mul(r, H.x, c.p, c.pinv);
-}
+__device__ __forceinline__ u64 half_enter(u64 r, const Prime& c, u64 x) { return mont_mul(r, x, c.p, c.pinv); }
 __device__ __forceinline__ u64 half_leave(u64 r, const Prime& c) {
     const u64 two_r2 = mod_add(c.r2, c.r2, c.p);
     return mont_mul(r, c.p - two_r2, c.p, c.pinv);
@@ -494,6 +492,74 @@ __device__ __forceinline__ u32 half_walk8x2(u32& al, u32& ah, u32& bl, u32& bh, 
         : "+r"(al), "+r"(ah), "+r"(bl), "+r"(bh), "=r"(flag)
         : "r"(k1), "r"(A.np0), "r"(A.np1), "r"(A.M), "r"(A.x0), "r"(A.x1), "r"(B.np0), "r"(B.np1), "r"(B.M),
           "r"(B.x0), "r"(B.x1));
+    return flag;
+}
+
+// ------------------------- iterate: lazy 96-bit steps, half-offset form --
+//
+// The half-offset form for the lazy 96-bit step (p k_max > 2^60).  With the
+// window z = t >> s taken one bit lower than the lazy 96-bit step takes it
+// (s = bitlen(p) + bitlen(k_max) - 29, so z < 2^30), the quotient falls
+// short by d < 2^s/p + z/2^32 < 2^(kb-28) + 1/4 <= 3/8 for k_max < 2^25:
+// r stays below (1 + d) p < x + p, and the exact test is r in {x, x + 1}.
+// Needs s >= 32 (bitlen(p) + bitlen(k_max) >= 61), which every p k_max
+// above 2^60 meets.
+struct Half96 {
+    u64 p, x;
+    u32 np0, np1, M, sh;      // 2^64 - p, floor(2^(32+s) / p), s - 32
+    u32 x0, x1;               // low words of x and x + 1
+};
+
+__device__ __forceinline__ bool half96_ok(u64 p, u32 kmax) {
+    return p > (1ull << 33) && (p >> 63) == 0 && kmax != 0 && bitlen32(kmax) <= 25 &&
+           bitlen64(p) + bitlen32(kmax) >= 61;
+}
+
+__device__ __forceinline__ Half96 make_half96(const Prime& c, u32 kmax) {
+    Half96 H;
+    H.p = c.p;
+    H.x = (c.p - 1) >> 1;
+    const u64 np = 0ull - c.p;
+    H.np0 = (u32)np;
+    H.np1 = (u32)(np >> 32);
+    const int s = bitlen64(c.p) + bitlen32(kmax) - 29;
+    H.sh = (u32)(s - 32);
+    H.M = recip_pow2(c.p, 32 + s);
+    H.x0 = (u32)H.x;
+    H.x1 = (u32)(H.x + 1);
+    return H;
+}
+
+__device__ __forceinline__ u64 half96_step(u64 r, u32 k, const Half96& H) {
+    const u64 lo = r * (u64)k, hi = __umul64hi(r, (u64)k);
+    const u32 q = __umulhi(top_bits(lo, hi, H.sh), H.M);
+    return lo + (u64)q * (((u64)H.np1 << 32) | H.np0);
+}
+__device__ __forceinline__ u64 half96_canon(u64 r, const Half96& H) { return r >= H.p ? r - H.p : r; }
+
+#define FS_H96_STEP2(J)                                                                        \
+    "add.u32 kk, %5, " #J ";\n\t"                                                              \
+    FS_HF_TEST("%0", "%10", "%11")                                                             \
+    FS_HF_TEST("%2", "%16", "%17")                                                             \
+    FS_L96_MUL("%0", "%1", "%6", "%7", "%8", "%9", "TA", "UA", "RA", "CA", "a0", "ac", "a1", "a2", "az", "aq") \
+    FS_L96_MUL("%2", "%3", "%12", "%13", "%14", "%15", "TB", "UB", "RB", "CB", "b0", "bc", "b1", "b2", "bz", "bq")
+
+__device__ __forceinline__ u32 half96_walk8x2(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const Half96& A,
+                                              const Half96& B) {
+    u32 flag;
+    asm("{\n\t"
+        ".reg .u32 kk, zr, a0, ac, a1, a2, az, aq, b0, bc, b1, b2, bz, bq;\n\t"
+        ".reg .u64 TA, UA, RA, CA, TB, UB, RB, CB;\n\t"
+        ".reg .pred P;\n\t"
+        "mov.u32 zr, 0;\n\t"
+        "setp.ne.u32 P, %5, %5;\n\t"
+        FS_H96_STEP2(0) FS_H96_STEP2(1) FS_H96_STEP2(2) FS_H96_STEP2(3)
+        FS_H96_STEP2(4) FS_H96_STEP2(5) FS_H96_STEP2(6) FS_H96_STEP2(7)
+        "selp.u32 %4, 1, 0, P;\n\t"
+        "}"
+        : "+r"(al), "+r"(ah), "+r"(bl), "+r"(bh), "=r"(flag)
+        : "r"(k1), "r"(A.np0), "r"(A.np1), "r"(A.M), "r"(A.sh), "r"(A.x0), "r"(A.x1),
+          "r"(B.np0), "r"(B.np1), "r"(B.M), "r"(B.sh), "r"(B.x0), "r"(B.x1));
     return flag;
 }
 

@@ -308,9 +308,23 @@ struct RegH64 {
     }
     static __device__ __forceinline__ u64 step(u64 r, u32 k, const K& X) { return half_step(r, k, X); }
     static __device__ __forceinline__ u64 canon(u64 r, const K& X) { return half_canon(r, X); }
-    static __device__ __forceinline__ u64 enter(u64 r, const Prime& c, const K& X) { return half_enter(r, c, X); }
+    static __device__ __forceinline__ u64 enter(u64 r, const Prime& c, const K& X) { return half_enter(r, c, X.x); }
     static __device__ __forceinline__ u64 leave(u64 r, const Prime& c, const K& X) {
         return half_leave(half_canon(r, X), c);
+    }
+    static __device__ __forceinline__ int hit(u64 c, const K& X) { return c == X.x ? -1 : (c == X.x + 1 ? 1 : 0); }
+};
+struct RegH96 {
+    using K = Half96;
+    static __device__ __forceinline__ K make(const Prime& c, u32 kmax) { return make_half96(c, kmax); }
+    static __device__ __forceinline__ u32 block(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const K& A, const K& B) {
+        return half96_walk8x2(al, ah, bl, bh, k1, A, B);
+    }
+    static __device__ __forceinline__ u64 step(u64 r, u32 k, const K& X) { return half96_step(r, k, X); }
+    static __device__ __forceinline__ u64 canon(u64 r, const K& X) { return half96_canon(r, X); }
+    static __device__ __forceinline__ u64 enter(u64 r, const Prime& c, const K& X) { return half_enter(r, c, X.x); }
+    static __device__ __forceinline__ u64 leave(u64 r, const Prime& c, const K& X) {
+        return half_leave(half96_canon(r, X), c);
     }
     static __device__ __forceinline__ int hit(u64 c, const K& X) { return c == X.x ? -1 : (c == X.x + 1 ? 1 : 0); }
 };
@@ -386,12 +400,13 @@ __device__ __forceinline__ u64 walk_generic(u64 r, const Prime& c, u32 nstart, u
     return r;
 }
 
-// Walk regime of one candidate for multipliers up to kmax: 4 lazy 64-bit in
-// half-offset form, 1 lazy 64-bit, 2 lazy 96-bit, 3 canonical 96-bit,
-// 0 generic Montgomery.
+// Walk regime of one candidate for multipliers up to kmax: 4 / 5 lazy 64-bit
+// / 96-bit in half-offset form, 1 lazy 64-bit, 2 lazy 96-bit, 3 canonical
+// 96-bit, 0 generic Montgomery.
 __device__ __forceinline__ int walk_regime(u64 p, u32 kmax) {
     if (half_ok(p, kmax)) return 4;
     if (lazy_ok(p, kmax)) return 1;
+    if (half96_ok(p, kmax)) return 5;
     if (lazy96_ok(p, kmax)) return 2;
     if (canon96_ok(p, kmax)) return 3;
     return 0;
@@ -404,6 +419,7 @@ __device__ __forceinline__ void walk_one(u64& r, const Prime& c, int reg, u32 ns
         case 2: walk_reg_pair<RegL96>(r, dup, c, c, false, nstart, nend, o); break;
         case 3: walk_reg_pair<RegC96>(r, dup, c, c, false, nstart, nend, o); break;
         case 4: walk_reg_pair<RegH64>(r, dup, c, c, false, nstart, nend, o); break;
+        case 5: walk_reg_pair<RegH96>(r, dup, c, c, false, nstart, nend, o); break;
         default: r = walk_generic(r, c, nstart, nend, o); break;
     }
 }
@@ -426,6 +442,7 @@ __device__ __forceinline__ void walk_pair(u64& ra, u64& rb, const Prime& a, cons
             case 1: walk_reg_pair<RegT64>(ra, rb, a, b, real_b, nstart, nend, o); return;
             case 2: walk_reg_pair<RegL96>(ra, rb, a, b, real_b, nstart, nend, o); return;
             case 4: walk_reg_pair<RegH64>(ra, rb, a, b, real_b, nstart, nend, o); return;
+            case 5: walk_reg_pair<RegH96>(ra, rb, a, b, real_b, nstart, nend, o); return;
             default: walk_reg_pair<RegC96>(ra, rb, a, b, real_b, nstart, nend, o); return;
         }
     }
@@ -438,6 +455,7 @@ __device__ __forceinline__ void walk_pair_as(u64& ra, u64& rb, const Prime& a, c
                                              u32 nstart, u32 nend, const WalkOut& o) {
     if (nstart >= nend) return;
     if (WALK == WALK_H64) walk_reg_pair<RegH64>(ra, rb, a, b, real_b, nstart, nend, o);
+    else if (WALK == WALK_H96) walk_reg_pair<RegH96>(ra, rb, a, b, real_b, nstart, nend, o);
     else if (WALK == WALK_T64) walk_reg_pair<RegT64>(ra, rb, a, b, real_b, nstart, nend, o);
     else if (WALK == WALK_L96) walk_reg_pair<RegL96>(ra, rb, a, b, real_b, nstart, nend, o);
     else if (WALK == WALK_C96) walk_reg_pair<RegC96>(ra, rb, a, b, real_b, nstart, nend, o);
@@ -513,6 +531,7 @@ __device__ __forceinline__ void walk_quad_as(u64 (&r)[4], Prime (&c)[4], u32 nre
                                              const WalkOut& o) {
     if (nstart >= nend) return;
     if (WALK == WALK_H64) walk_reg4<RegH64>(r, c, nreal, nstart, nend, o);
+    else if (WALK == WALK_H96) walk_reg4<RegH96>(r, c, nreal, nstart, nend, o);
     else if (WALK == WALK_T64) walk_reg4<RegT64>(r, c, nreal, nstart, nend, o);
     else if (WALK == WALK_L96) walk_reg4<RegL96>(r, c, nreal, nstart, nend, o);
     else if (WALK == WALK_C96) walk_reg4<RegC96>(r, c, nreal, nstart, nend, o);
@@ -528,6 +547,7 @@ __device__ __forceinline__ void walk_quad_rt(int walk, u64 (&r)[4], Prime (&c)[4
                                              const WalkOut& o) {
     switch (walk) {
         case WALK_H64: walk_quad_as<WALK_H64>(r, c, nreal, nstart, nend, o); break;
+        case WALK_H96: walk_quad_as<WALK_H96>(r, c, nreal, nstart, nend, o); break;
         case WALK_T64: walk_quad_as<WALK_T64>(r, c, nreal, nstart, nend, o); break;
         case WALK_L96: walk_quad_as<WALK_L96>(r, c, nreal, nstart, nend, o); break;
         case WALK_C96: walk_quad_as<WALK_C96>(r, c, nreal, nstart, nend, o); break;
@@ -1038,7 +1058,8 @@ __global__ void __launch_bounds__(256) imad_bench_kernel(u32 iters, u32 kind, u3
 //   kind 7  lazy 96-bit steps (lazy96_walk8x2), 4 chains
 //   kind 8  canonical 96-bit steps (canon96_walk8x2), 4 chains
 //   kind 9  generic Montgomery steps (mont_mul by kR, k advanced by R), 4 chains
-constexpr u32 kCeilUnits[10] = {0, 0, 0, 0, 8, 32, 32, 32, 32, 4};
+//   kind 10 half-offset lazy 96-bit steps (half96_walk8x2), 4 chains
+constexpr u32 kCeilUnits[11] = {0, 0, 0, 0, 8, 32, 32, 32, 32, 4, 32};
 
 template <u32 kind>
 __global__ void __launch_bounds__(256) ceiling_kernel(u32 iters, u32 seed, u32* sink) {
@@ -1049,6 +1070,7 @@ __global__ void __launch_bounds__(256) ceiling_kernel(u32 iters, u32 seed, u32* 
         case 5: base = 1000000000000ull; break;           // p kmax <= 2^60
         case 6: base = (1ull << 34) + 1; break;           // 2^33 < p, p kmax <= 2^62
         case 7: base = 1000000000000000ull; break;        // p kmax > 2^62, p < 2^63
+        case 10: base = 1000000000000000ull; break;       // p kmax > 2^60, p < 2^63
         case 8: base = (1ull << 63) + 1; break;           // p >= 2^63
         default: base = (1ull << 63) + 1; break;
     }
@@ -1103,6 +1125,14 @@ __global__ void __launch_bounds__(256) ceiling_kernel(u32 iters, u32 seed, u32* 
             for (u32 it = 0; it < iters; ++it) {
                 acc += lazy_walk8x2(l[0], hh[0], l[1], hh[1], k0 + 8 * it, A, B);
                 acc += lazy_walk8x2(l[2], hh[2], l[3], hh[3], k0 + 8 * it, C, D);
+            }
+        } else if constexpr (kind == 10) {
+            const u32 kmax = k0 + 8 * iters;
+            const Half96 A = make_half96(c[0], kmax), B = make_half96(c[1], kmax);
+            const Half96 C = make_half96(c[2], kmax), D = make_half96(c[3], kmax);
+            for (u32 it = 0; it < iters; ++it) {
+                acc += half96_walk8x2(l[0], hh[0], l[1], hh[1], k0 + 8 * it, A, B);
+                acc += half96_walk8x2(l[2], hh[2], l[3], hh[3], k0 + 8 * it, C, D);
             }
         } else if constexpr (kind == 7) {
             const u32 kmax = k0 + 8 * iters;
@@ -1164,6 +1194,8 @@ cudaError_t launch_sieve(const SieveArgs& a, int setup, bool final_chunk, int gr
         switch (walk * 2 + (variant == 6)) {
             case WALK_H64 * 2: launch_sieve_w<2, WALK_H64, 4>(a, setup, final_chunk, grid, s); break;
             case WALK_H64 * 2 + 1: launch_sieve_w<3, WALK_H64, 4>(a, setup, final_chunk, grid, s); break;
+            case WALK_H96 * 2: launch_sieve_w<2, WALK_H96, 4>(a, setup, final_chunk, grid, s); break;
+            case WALK_H96 * 2 + 1: launch_sieve_w<3, WALK_H96, 4>(a, setup, final_chunk, grid, s); break;
             case WALK_T64 * 2: launch_sieve_w<2, WALK_T64, 4>(a, setup, final_chunk, grid, s); break;
             case WALK_L96 * 2: launch_sieve_w<2, WALK_L96, 4>(a, setup, final_chunk, grid, s); break;
             case WALK_C96 * 2: launch_sieve_w<2, WALK_C96, 4>(a, setup, final_chunk, grid, s); break;
@@ -1175,6 +1207,7 @@ cudaError_t launch_sieve(const SieveArgs& a, int setup, bool final_chunk, int gr
     } else {
         switch (walk) {
             case WALK_H64: launch_sieve_w<3, WALK_H64>(a, setup, final_chunk, grid, s); break;
+            case WALK_H96: launch_sieve_w<3, WALK_H96>(a, setup, final_chunk, grid, s); break;
             case WALK_T64: launch_sieve_w<3, WALK_T64>(a, setup, final_chunk, grid, s); break;
             case WALK_L96: launch_sieve_w<3, WALK_L96>(a, setup, final_chunk, grid, s); break;
             case WALK_C96: launch_sieve_w<3, WALK_C96>(a, setup, final_chunk, grid, s); break;
@@ -1224,12 +1257,13 @@ cudaError_t launch_imad_bench(u32 iters, u32 kind, u32 seed, u32* sink, int grid
         case 7: ceiling_kernel<7><<<grid, 256, 0, s>>>(iters, seed, sink); break;
         case 8: ceiling_kernel<8><<<grid, 256, 0, s>>>(iters, seed, sink); break;
         case 9: ceiling_kernel<9><<<grid, 256, 0, s>>>(iters, seed, sink); break;
+        case 10: ceiling_kernel<10><<<grid, 256, 0, s>>>(iters, seed, sink); break;
         default: imad_bench_kernel<<<grid, 256, 0, s>>>(iters, kind, seed, sink); break;
     }
     return cudaGetLastError();
 }
 
-double bench_units_per_thread_iter(u32 kind) { return kind < 4 ? 8.0 : (kind < 10 ? kCeilUnits[kind] : 0.0); }
+double bench_units_per_thread_iter(u32 kind) { return kind < 4 ? 8.0 : (kind < 11 ? kCeilUnits[kind] : 0.0); }
 
 int walk_for_range(uint64_t plo, uint64_t phi, uint32_t kmax) {
     if (phi <= plo || kmax == 0) return WALK_ANY;
@@ -1239,6 +1273,10 @@ int walk_for_range(uint64_t plo, uint64_t phi, uint32_t kmax) {
     if (plo >= (1ull << 36) && pmax <= ((1ull << 60) / kmax)) return WALK_H64;
     // the lazy 64-bit step needs p > 2^33 and p kmax <= 2^62 (lazy_ok)
     if (plo > (1ull << 33) && pmax <= ((1ull << 62) / kmax)) return WALK_T64;
+    // the half-offset lazy 96-bit step needs 2^33 < p < 2^63, kmax < 2^25 and
+    // bitlen(p) + bitlen(kmax) >= 61 (half96_ok)
+    if (kb <= 25 && plo > (1ull << 33) && (pmax >> 63) == 0 && (64 - __builtin_clzll(plo)) + kb >= 61)
+        return WALK_H96;
     if (kb <= 28 && plo > (1ull << 33) && (pmax >> 63) == 0) return WALK_L96;
     if (kb <= 28 && (plo >> 63) != 0) return WALK_C96;
     return WALK_ANY;

@@ -195,7 +195,8 @@ def test_hit_overflow_is_reported(ctx):
 
 
 @pytest.mark.parametrize("lo,hi,nmin,nmax", [
-    (10**15, 10**15 + 300_000, 100_000, 100_700),                  # lazy 96-bit step (p < 2^63, p k > 2^62)
+    (10**15, 10**15 + 300_000, 100_000, 100_700),                  # half-offset 96-bit step (p < 2^63, p k > 2^62)
+    (10**13, 10**13 + 30_000, 40_000_000, 40_000_500),             # lazy 96-bit step (k_max >= 2^25)
     ((1 << 63) + 1, (1 << 63) + 300_000, 5_000, 5_700),             # canonical 96-bit step (p >= 2^63)
     ((1 << 64) - 400_000, (1 << 64) - 1, 1_000, 1_333),              # canonical 96-bit step near 2^64
     (4 * 10**12, 4 * 10**12 + 200_000, 1_000_000, 1_000_300),      # across the 64/96-bit boundary
@@ -277,6 +278,7 @@ def test_four_candidate_kernel_reference_selftests(ctx, variant, case):
     ((1 << 63) + 1, (1 << 63) + 300_001, 5_000, 5_700),             # canonical 96-bit walk
     ((1 << 64) - 400_000, (1 << 64) - 1, 1_000, 1_333),              # canonical 96-bit walk near 2^64
     (4 * 10**12, 4 * 10**12 + 200_000, 1_000_000, 1_000_300),      # mixed steps: pairs one after the other
+    (10**15 + 1, 10**15 + 300_001, 100_000, 100_701),               # half-offset 96-bit walk
     (10**12 + 7, 10**12 + 300_007, 100_000, 100_701),               # lazy 64-bit, odd n-range (tail steps)
     ((1 << 33) - 150_000, (1 << 33) + 150_000, 2000, 2900),         # generic / lazy boundary
 ])
