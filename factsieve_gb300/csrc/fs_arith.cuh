@@ -424,10 +424,12 @@ __device__ __forceinline__ u32 canon96_walk8x2(u32& al, u32& ah, u32& bl, u32& b
 // n! = -1 gives -x = x + 1, two adjacent values.  The quotient estimate of
 // the lazy step falls short of floor(t/p) by at most one, and only when
 // t mod p < d p with d < 2^32/p + z/2^32 (z = t >> 32): the step leaves r in
-// [0, (1 + d) p).  For p >= 2^36 and p kmax <= 2^60 (r < 2p, z < 2p kmax /
-// 2^32) d < 1/16 + 1/8 < 1/2, so r never reaches x + p or x + 1 + p and the
-// exact hit test is r in {x, x + 1}: two compares of the low word per step
-// instead of the four the [0, 2p) window needs.
+// [0, (1 + d) p).  If r < (1 + e) p then z < (1 + e) p kmax / 2^32, so for
+// p >= 2^36 and p kmax <= 2^62, d < 1/16 + (1 + e)/4, whose fixed point is
+// e = 5/12: starting canonical, r stays below (17/12) p < x + p, never
+// reaches x + p or x + 1 + p, and the exact hit test is r in {x, x + 1}: two
+// compares of the low word per step instead of the four the [0, 2p) window
+// needs.
 struct Half64 {
     u64 p, x;                 // x = (p - 1) / 2
     u32 np0, np1, M;          // 2^64 - p (two words), floor(2^64 / p)
@@ -435,7 +437,7 @@ struct Half64 {
 };
 
 __device__ __forceinline__ bool half_ok(u64 p, u32 kmax) {
-    return p >= (1ull << 36) && p <= ((1ull << 60) / (u64)(kmax ? kmax : 1));
+    return p >= (1ull << 36) && p <= ((1ull << 62) / (u64)(kmax ? kmax : 1));
 }
 
 __device__ __forceinline__ Half64 make_half(const Prime& c) {

@@ -1269,8 +1269,8 @@ int walk_for_range(uint64_t plo, uint64_t phi, uint32_t kmax) {
     if (phi <= plo || kmax == 0) return WALK_ANY;
     const uint64_t pmax = phi - 1;
     const int kb = 32 - __builtin_clz(kmax);
-    // the half-offset lazy step needs p >= 2^36 and p kmax <= 2^60 (half_ok)
-    if (plo >= (1ull << 36) && pmax <= ((1ull << 60) / kmax)) return WALK_H64;
+    // the half-offset lazy step needs p >= 2^36 and p kmax <= 2^62 (half_ok)
+    if (plo >= (1ull << 36) && pmax <= ((1ull << 62) / kmax)) return WALK_H64;
     // the lazy 64-bit step needs p > 2^33 and p kmax <= 2^62 (lazy_ok)
     if (plo > (1ull << 33) && pmax <= ((1ull << 62) / kmax)) return WALK_T64;
     // the half-offset lazy 96-bit step needs 2^33 < p < 2^63, kmax < 2^25 and

@@ -205,7 +205,8 @@ def test_hit_overflow_is_reported(ctx):
     ((1 << 33) - 150_000, (1 << 33) + 150_000, 2000, 2900),         # generic / lazy boundary at 2^33
     (8 * 10**12, 8 * 10**12 + 300_000, 524_000, 524_400),          # multipliers across 2^19
     ((1 << 36) - 150_000, (1 << 36) + 150_000, 2000, 2900),         # lazy / half-offset boundary at p = 2^36
-    ((1 << 40) - 150_000, (1 << 40) + 150_000, 1_047_700, 1 << 20),    # half-offset limit p kmax = 2^60
+    ((1 << 40) - 150_000, (1 << 40) + 150_000, 1_047_700, 1 << 20),    # p kmax = 2^60
+    ((1 << 40) - 50_000, (1 << 40) + 50_000, 4_193_800, 1 << 22),      # half-offset 64-bit limit p kmax = 2^62
 ])
 def test_walk_regimes_match_oracle(ctx, orc, lo, hi, nmin, nmax):
     """Every walk regime (and a pair straddling two) gives the oracle's residues, sums and hits."""
@@ -297,7 +298,7 @@ def test_four_candidate_kernel_matches_oracle(ctx, orc, variant, lo, hi, nmin, n
 
 # Prime factors p >= 2^36 of n! + c for small n (found by factoring n! +- 1;
 # each is re-checked below with an exact factorial): real hits for the
-# lazy walks, including the half-offset form (p >= 2^36, p kmax <= 2^60).
+# lazy walks, including the half-offset forms.
 KNOWN_FACTORS = [(87178291199, 14, -1), (256443711677, 17, -1), (1713311273363831, 19, 1),
                  (117876683047, 20, 1), (19499250680671, 20, -1), (2703875815783, 21, 1),
                  (4826713612027, 21, -1), (93799610095769647, 22, 1), (170006681813, 22, -1),
