@@ -499,13 +499,13 @@ __device__ __forceinline__ u32 half_walk8x2(u32& al, u32& ah, u32& bl, u32& bh, 
 
 // ------------------------- iterate: lazy 96-bit steps, half-offset form --
 //
-// The half-offset form for the lazy 96-bit step (p k_max > 2^60).  With the
-// window z = t >> s taken one bit lower than the lazy 96-bit step takes it
-// (s = bitlen(p) + bitlen(k_max) - 29, so z < 2^30), the quotient falls
-// short by d < 2^s/p + z/2^32 < 2^(kb-28) + 1/4 <= 3/8 for k_max < 2^25:
-// r stays below (1 + d) p < x + p, and the exact test is r in {x, x + 1}.
-// Needs s >= 32 (bitlen(p) + bitlen(k_max) >= 61), which every p k_max
-// above 2^60 meets.
+// The half-offset form for the lazy 96-bit step.  With the window z = t >> s
+// taken one bit lower than the lazy 96-bit step takes it (s = bitlen(p) +
+// bitlen(k_max) - 29), the quotient falls short by d < 2^s/p + z/2^32.  If
+// r < (1 + e) p then z < (1 + e) 2^29, so for k_max < 2^26 d < 1/4 +
+// (1 + e)/8, whose fixed point is e = 3/7: r stays below (10/7) p < x + p,
+// and the exact test is r in {x, x + 1}.  Needs s >= 32 (bitlen(p) +
+// bitlen(k_max) >= 61), which every p k_max above 2^60 meets.
 struct Half96 {
     u64 p, x;
     u32 np0, np1, M, sh;      // 2^64 - p, floor(2^(32+s) / p), s - 32
@@ -513,7 +513,7 @@ struct Half96 {
 };
 
 __device__ __forceinline__ bool half96_ok(u64 p, u32 kmax) {
-    return p > (1ull << 33) && (p >> 63) == 0 && kmax != 0 && bitlen32(kmax) <= 25 &&
+    return p > (1ull << 33) && (p >> 63) == 0 && kmax != 0 && bitlen32(kmax) <= 26 &&
            bitlen64(p) + bitlen32(kmax) >= 61;
 }
 

@@ -1273,9 +1273,9 @@ int walk_for_range(uint64_t plo, uint64_t phi, uint32_t kmax) {
     if (plo >= (1ull << 36) && pmax <= ((1ull << 62) / kmax)) return WALK_H64;
     // the lazy 64-bit step needs p > 2^33 and p kmax <= 2^62 (lazy_ok)
     if (plo > (1ull << 33) && pmax <= ((1ull << 62) / kmax)) return WALK_T64;
-    // the half-offset lazy 96-bit step needs 2^33 < p < 2^63, kmax < 2^25 and
+    // the half-offset lazy 96-bit step needs 2^33 < p < 2^63, kmax < 2^26 and
     // bitlen(p) + bitlen(kmax) >= 61 (half96_ok)
-    if (kb <= 25 && plo > (1ull << 33) && (pmax >> 63) == 0 && (64 - __builtin_clzll(plo)) + kb >= 61)
+    if (kb <= 26 && plo > (1ull << 33) && (pmax >> 63) == 0 && (64 - __builtin_clzll(plo)) + kb >= 61)
         return WALK_H96;
     if (kb <= 28 && plo > (1ull << 33) && (pmax >> 63) == 0) return WALK_L96;
     if (kb <= 28 && (plo >> 63) != 0) return WALK_C96;

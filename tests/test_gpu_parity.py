@@ -196,7 +196,8 @@ def test_hit_overflow_is_reported(ctx):
 
 @pytest.mark.parametrize("lo,hi,nmin,nmax", [
     (10**15, 10**15 + 300_000, 100_000, 100_700),                  # half-offset 96-bit step (p < 2^63, p k > 2^62)
-    (10**13, 10**13 + 30_000, 40_000_000, 40_000_500),             # lazy 96-bit step (k_max >= 2^25)
+    (10**13, 10**13 + 30_000, 67_109_000, 67_109_700),             # lazy 96-bit step (k_max >= 2^26)
+    (10**13, 10**13 + 30_000, 67_108_000, 67_108_800),             # half-offset 96-bit step, k_max just below 2^26
     ((1 << 63) + 1, (1 << 63) + 300_000, 5_000, 5_700),             # canonical 96-bit step (p >= 2^63)
     ((1 << 64) - 400_000, (1 << 64) - 1, 1_000, 1_333),              # canonical 96-bit step near 2^64
     (4 * 10**12, 4 * 10**12 + 200_000, 1_000_000, 1_000_300),      # across the 64/96-bit boundary
