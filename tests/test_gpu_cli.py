@@ -120,3 +120,22 @@ def test_cli_top_of_the_p_range(fslib, orc, tmp_path):
     got = (tmp_path / "factors.txt").read_text().splitlines()
     assert got == (lines or ["no factors"]) + [f"{want['checksum']:016X}"]
     assert f"prime count {want['primecount']}," in r.stdout
+
+
+@pytest.mark.parametrize("name,argv", [
+    ("config2", ["-n", "1e5", "-N", "2e5", "-p", "1e12", "-P", "1001e9"]),          # the survey's own spelling
+    ("config3", ["-n", "1e6", "-N", "101e4", "-p", "9223372036854775808", "-P", "9223372037854775808"]),
+])
+def test_cli_full_config_matches_oracle_fixture(fslib, tmp_path, name, argv):
+    """The drop-in CLI over a whole benchmark configuration (1e9-wide p-range):
+    factors.txt and the final line equal the oracle's output for the same range
+    (tests/golden/run_<name>.json)."""
+    path = os.path.join(GOLD, f"run_{name}.json")
+    if not os.path.exists(path):
+        pytest.skip(f"fixture {name} not generated")
+    g = _gold(name)
+    r = _cli(fslib, argv + ["-v", "16"], tmp_path)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    lines = (tmp_path / "factors.txt").read_text().splitlines()
+    assert lines == (g["factors"] or ["no factors"]) + [g["checksum"]]
+    assert f"factors {g['factorcount']}, prime count {g['primecount']}, checksum {g['checksum']}" in r.stdout
