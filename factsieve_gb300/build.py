@@ -26,7 +26,8 @@ CLI = os.path.join(HERE, "bin", "factsieve")
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["fs_kernels.cu", "fs_capi.cu", "fs_noalloc.cu", "fs_serve.cu"]
+CU_SOURCES = ["fs_kernels.cu", "fs_sieve2.cu", "fs_sieve4.cu", "fs_multi.cu", "fs_capi.cu", "fs_noalloc.cu",
+              "fs_serve.cu"]
 CXX_SOURCES = ["fs_host.cpp", "fs_post.cpp", "fs_putil.cpp"]
 CLI_SOURCES = ["factsieve_main.cpp", "search.cpp"]
 

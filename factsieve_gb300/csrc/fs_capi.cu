@@ -161,23 +161,20 @@ fs::SieveArgs base_args(PlanGPU* pl) {
     return a;
 }
 
-// Sieve kernel build (fs_tuning.sieve_variant): 2..4 two candidates per
-// thread at that many resident blocks per SM, 5 / 6 four candidates per
-// thread at 2 / 3.  The default is 5, which the measurements favour on every
-// segment whose candidates share one walk step (the usual case).
-int variant(fs_ctx* c) {
-    const uint32_t v = c->tuning.sieve_variant;
-    return (v >= 2 && v <= 6) ? (int)v : 5;
-}
+// Sieve kernel build (fs_tuning.sieve_variant): 3 two candidates per thread
+// at 3 resident blocks per SM, 5 four candidates per thread at 2.  The
+// default is 5, which the measurements favour on every segment whose
+// candidates share one walk step (the usual case).
+int variant(fs_ctx* c) { return c->tuning.sieve_variant == 3 ? 3 : 5; }
 
 // The build a launch really runs: the four-candidate kernels exist for the
-// specialised walks only; a mixed segment (WALK_ANY) runs variant 3.
-int kernel_variant(int v, int walk) { return ((v == 5 || v == 6) && walk == fs::WALK_ANY) ? 3 : v; }
+// launch-wide walks only; a mixed segment (WALK_ANY) runs variant 3.
+int kernel_variant(int v, int walk) { return (v == 5 && walk == fs::WALK_ANY) ? 3 : v; }
 
 // Default blocks per SM for a build: its resident occupancy, and for the
-// four-candidate builds four times that, so the candidates are dealt in
+// four-candidate build four times that, so the candidates are dealt in
 // smaller shares and the last wave is short.
-int default_bpsm(fs_ctx* c, int kv) { return c->sieve_occ[kv] * ((kv == 5 || kv == 6) ? 4 : 1); }
+int default_bpsm(fs_ctx* c, int kv) { return c->sieve_occ[kv] * (kv == 5 ? 4 : 1); }
 
 // The build for launches that walk each candidate with its own step.
 int any_variant(fs_ctx* c) { return kernel_variant(variant(c), fs::WALK_ANY); }
@@ -407,7 +404,7 @@ int fs_create(int device, fs_ctx** out) {
     cudaDeviceGetAttribute(&clk, cudaDevAttrClockRate, device);
     c->clock_khz = clk;
     c->total_mem = prop.totalGlobalMem;
-    for (int v = 2; v <= 6; ++v) {
+    for (int v : {3, 5}) {
         int occ = 0;
         if (fs::sieve_occupancy(&occ, v) == cudaSuccess && occ > 0) c->sieve_occ[v] = occ;
     }

@@ -123,6 +123,10 @@ cudaError_t batch_occupancy(int* blocks_per_sm);
 int batch_max_jobs();
 cudaError_t launch_sieve(const SieveArgs& a, int setup, bool final_chunk, int grid, cudaStream_t s, int variant,
                          int walk);
+cudaError_t launch_sieve_pair(const SieveArgs& a, int setup, bool final_chunk, int grid, cudaStream_t s, int walk);
+cudaError_t launch_sieve_quad(const SieveArgs& a, int setup, bool final_chunk, int grid, cudaStream_t s, int walk);
+cudaError_t sieve_pair_occupancy(int* blocks_per_sm);
+cudaError_t sieve_quad_occupancy(int* blocks_per_sm);
 // The walk step valid for every p in [plo, phi) with multipliers up to kmax.
 int walk_for_range(uint64_t plo, uint64_t phi, uint32_t kmax);
 cudaError_t launch_setup_partial(const SieveArgs& a, int grid_x, int nchunks, cudaStream_t s);

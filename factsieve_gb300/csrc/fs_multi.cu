@@ -1,0 +1,230 @@
+// fs_multi.cu -- the batch kernel (many uneven jobs in one persistent launch)
+// and the serving-round kernel (chunks of resident jobs), four candidates
+// per thread with each job's walk step chosen at run time.
+#include "fs_walk.cuh"
+
+namespace fs {
+
+// ============================================================ batches ====
+
+// Persistent kernel over many uneven jobs.  A tile is kTileCandidates
+// candidates of one job, four per thread; blocks take tiles from a global
+// counter until the batch is done.  The host orders jobs by estimated work
+// per candidate, heaviest first, so the long tiles start early and the tail
+// is made of short ones.  Each job carries the walk step valid for its whole
+// p-range, uniform over a tile.
+constexpr int kBatchMaxJobs = 1024;
+
+__global__ void __launch_bounds__(kSieveThreads, 2) batch_sieve_kernel(BatchArgs a) {
+    __shared__ HitStage st;
+    __shared__ u32 tile_end[kBatchMaxJobs];   // inclusive prefix sum of tiles per job
+    __shared__ u32 s_tile;
+    __shared__ u64 wsum[kSieveThreads / 32];
+    __shared__ u32 wbad[kSieveThreads / 32];
+    const u32 per_tile = kTileCandidates;
+    if (threadIdx.x == 0) {
+        st.n = 0;
+        u32 acc = 0;
+        for (u32 j = 0; j < a.njobs; ++j) {
+            const u32 nc = a.ctr[j].ncand;
+            const u32 n = nc < a.jobs[j].cap ? nc : a.jobs[j].cap;
+            acc += (n + per_tile - 1) / per_tile;
+            tile_end[j] = acc;
+        }
+    }
+    __syncthreads();
+    const u32 total = tile_end[a.njobs - 1];
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(a.tile_counter, 1u);
+        __syncthreads();
+        const u32 t = s_tile;
+        __syncthreads();
+        if (t >= total) break;
+        // job of tile t: first j with tile_end[j] > t (binary search)
+        u32 lo = 0, hi = a.njobs - 1;
+        while (lo < hi) {
+            const u32 mid = (lo + hi) >> 1;
+            if (tile_end[mid] > t) hi = mid;
+            else lo = mid + 1;
+        }
+        const u32 j = lo;
+        const BatchJob& J = a.jobs[j];
+        const u32 nc = a.ctr[j].ncand;
+        const u32 n = nc < J.cap ? nc : J.cap;
+        const u32 i0 = (t - (j ? tile_end[j - 1] : 0)) * per_tile + 4 * threadIdx.x;
+        u64 sum = 0;
+        u32 bad = 0;
+        if (i0 < n) {
+            const WalkOut o{&st, a.hits, a.hitcap, a.gctr, (int)j};
+            Prime c[4];
+            const u32 nreal = load_quad(J.cand, i0, n, c);
+            u64 r[4];
+            plan_product4(c, a.words, a.layers, J.layer_begin, J.layer_end, r);
+#pragma unroll
+            for (int h = 0; h < 4; ++h) r[h] = mont_mul(r[h], mont_pow(c[h].r2, J.deficit, c[h]), c[h].p, c[h].pinv);
+            walk_quad_rt((int)J.walk, r, c, nreal, J.nstart, J.nend, o);
+#pragma unroll
+            for (int h = 0; h < 4; ++h)
+                if ((u32)h < nreal) final_check(c[h], r[h], J.nend, sum, bad);
+        }
+#pragma unroll
+        for (int d = 16; d; d >>= 1) {
+            sum += __shfl_xor_sync(0xffffffffu, sum, d);
+            bad += __shfl_xor_sync(0xffffffffu, bad, d);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            wsum[threadIdx.x >> 5] = sum;
+            wbad[threadIdx.x >> 5] = bad;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            u64 s = 0;
+            u32 b = 0;
+            for (int w = 0; w < (int)(blockDim.x / 32); ++w) {
+                s += wsum[w];
+                b += wbad[w];
+            }
+            if (s) atomicAdd(&a.ctr[j].raw_sum, s);
+            if (b) atomicOr(&a.ctr[j].flags, FLAG_VALIDATION);
+        }
+    }
+    __syncthreads();
+    const u32 nh = st.n < kHitStage ? st.n : kHitStage;
+    if (nh) {
+        __shared__ u32 gbase;
+        if (threadIdx.x == 0) gbase = atomicAdd(&a.gctr->nhits, nh);
+        __syncthreads();
+        for (u32 k = threadIdx.x; k < nh; k += blockDim.x) {
+            const u32 g = gbase + k;
+            if (g < a.hitcap)
+                a.hits[g] = st.buf[k];
+            else
+                atomicOr(&a.gctr->flags, FLAG_HIT_OVERFLOW);
+        }
+    }
+}
+
+// ============================================================ serving ====
+
+// One round of the serving loop: a list of tiles, each up to kTileCandidates
+// candidates of one job in one phase (starting residue from the plan, a
+// chunk of the walk, the final checksum), four per thread, taken from a
+// global counter by persistent blocks.  Residues live in each job's device
+// buffer between rounds.
+__global__ void __launch_bounds__(kSieveThreads, 2) serve_round_kernel(ServeArgs a) {
+    __shared__ HitStage st;
+    __shared__ u32 s_tile;
+    __shared__ u64 wsum[kSieveThreads / 32];
+    __shared__ u32 wbad[kSieveThreads / 32];
+    if (threadIdx.x == 0) st.n = 0;
+    __syncthreads();
+    const u32 per_tile = kTileCandidates;
+    const u32 ntiles = a.nchunks ? a.chunks[a.nchunks - 1].tile_end : 0;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(a.tile_counter, 1u);
+        __syncthreads();
+        const u32 t = s_tile;
+        __syncthreads();
+        if (t >= ntiles) break;
+        // chunk of tile t: first c with tile_end > t
+        u32 lo = 0, hi = a.nchunks - 1;
+        while (lo < hi) {
+            const u32 mid = (lo + hi) >> 1;
+            if (a.chunks[mid].tile_end > t) hi = mid;
+            else lo = mid + 1;
+        }
+        const ServeChunk T = a.chunks[lo];
+        const u32 tile0 = lo ? a.chunks[lo - 1].tile_end : 0;
+        const u32 i0 = T.first + (t - tile0) * per_tile + 4 * threadIdx.x;
+        const u32 end = T.first + T.count;
+        u64 sum = 0;
+        u32 bad = 0;
+        if (i0 < end) {
+            const WalkOut o{&st, a.hits, a.hitcap, a.gctr, (int)T.tag};
+            Prime c[4];
+            const u32 nreal = load_quad(T.cand, i0, end, c);
+            u64 r[4];
+            if (T.flags & SERVE_SETUP) {
+                plan_product4(c, T.words, T.layers, T.layer_begin, T.layer_end, r);
+#pragma unroll
+                for (int h = 0; h < 4; ++h)
+                    r[h] = mont_mul(r[h], mont_pow(c[h].r2, T.deficit, c[h]), c[h].p, c[h].pinv);
+            } else {
+                r[0] = T.residue[i0];
+#pragma unroll
+                for (int h = 1; h < 4; ++h) r[h] = (u32)h < nreal ? T.residue[i0 + h] : r[0];
+            }
+            walk_quad_rt((int)T.walk, r, c, nreal, T.nstart, T.nend, o);
+            if (T.flags & SERVE_FINAL) {
+#pragma unroll
+                for (int h = 0; h < 4; ++h)
+                    if ((u32)h < nreal) final_check(c[h], r[h], T.nend, sum, bad);
+            } else {
+#pragma unroll
+                for (int h = 0; h < 4; ++h)
+                    if ((u32)h < nreal) T.residue[i0 + h] = r[h];
+            }
+        }
+    if (T.flags & SERVE_FINAL) {
+#pragma unroll
+            for (int d = 16; d; d >>= 1) {
+                sum += __shfl_xor_sync(0xffffffffu, sum, d);
+                bad += __shfl_xor_sync(0xffffffffu, bad, d);
+            }
+            if ((threadIdx.x & 31) == 0) {
+                wsum[threadIdx.x >> 5] = sum;
+                wbad[threadIdx.x >> 5] = bad;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                u64 s = 0;
+                u32 b = 0;
+                for (int w = 0; w < (int)(blockDim.x / 32); ++w) {
+                    s += wsum[w];
+                    b += wbad[w];
+                }
+                if (s) atomicAdd(&T.ctr->raw_sum, s);
+                if (b) atomicOr(&T.ctr->flags, FLAG_VALIDATION);
+            }
+        }
+    }
+    __syncthreads();
+    const u32 nh = st.n < kHitStage ? st.n : kHitStage;
+    if (nh) {
+        __shared__ u32 gbase;
+        if (threadIdx.x == 0) gbase = atomicAdd(&a.gctr->nhits, nh);
+        __syncthreads();
+        for (u32 k = threadIdx.x; k < nh; k += blockDim.x) {
+            const u32 g = gbase + k;
+            if (g < a.hitcap)
+                a.hits[g] = st.buf[k];
+            else
+                atomicOr(&a.gctr->flags, FLAG_HIT_OVERFLOW);
+        }
+    }
+}
+
+// ============================================================== launches ===
+
+cudaError_t launch_batch(const BatchArgs& a, int grid, cudaStream_t s) {
+    if (a.njobs == 0 || a.njobs > (u32)kBatchMaxJobs) return cudaErrorInvalidValue;
+    batch_sieve_kernel<<<grid, kSieveThreads, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t batch_occupancy(int* blocks_per_sm) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, batch_sieve_kernel, kSieveThreads, 0);
+}
+
+int batch_max_jobs() { return kBatchMaxJobs; }
+
+cudaError_t launch_serve_round(const ServeArgs& a, int grid, cudaStream_t s) {
+    serve_round_kernel<<<grid, kSieveThreads, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t serve_occupancy(int* blocks_per_sm) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, serve_round_kernel, kSieveThreads, 0);
+}
+
+}  // namespace fs

@@ -3,8 +3,8 @@
 Knobs (fs_tuning in include/factsieve.h):
   sieve_variant         the sieve kernel build: 3 = two candidates per thread
                         at 3 resident 256-thread blocks per SM (register cap
-                        85), 5 / 6 = four candidates per thread (two
-                        interleaved pairs) at 2 / 3 blocks per SM
+                        85), 5 = four candidates per thread (two interleaved
+                        pairs) at 2 blocks per SM
   sieve_blocks_per_sm   blocks launched per SM (beyond the resident ones they
                         run as later waves, which evens out the last wave)
   segment width         p-width of one launch (candidates per launch: larger
@@ -62,7 +62,7 @@ class TuningCache:
             os.replace(tmp, self.path)
 
 
-VARIANTS = (3, 5, 6)
+VARIANTS = (3, 5)
 
 
 def candidates(default_blocks_by_variant):

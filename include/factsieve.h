@@ -68,9 +68,9 @@ typedef struct {
     uint32_t gen_blocks_per_sm;     /* candidate-generator blocks per SM */
     uint32_t max_steps_per_launch;  /* split the n-range into launches of at most this many steps */
     uint32_t setup_chunks;          /* split the power table across this many threads per prime (1 = never) */
-    uint32_t sieve_variant;         /* sieve kernel build: 2, 3 or 4 resident blocks per SM (register cap) with two
-                                       candidates per thread; 5 / 6: four candidates per thread at 2 / 3 blocks
-                                       per SM (segments whose candidates share one walk step; else variant 3) */
+    uint32_t sieve_variant;         /* sieve kernel build: 3 = two candidates per thread at 3 resident blocks per
+                                       SM; 5 (default) = four candidates per thread at 2 (segments whose
+                                       candidates share one walk step; a mixed segment runs build 3) */
 } fs_tuning;
 
 /* ---- library / device ---------------------------------------------------- */

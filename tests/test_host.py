@@ -128,3 +128,23 @@ def test_context_needs_a_device(fslib):
         pytest.skip("a device is present")
     with pytest.raises(fslib.FSError):
         fslib.Context(0)
+
+
+def test_walk_step_selection_boundaries(fslib):
+    """The launch-wide step the host proves valid for a p-segment (fs_walk_step)."""
+    H64, T64, L96, C96, H96, ANY = 4, 1, 2, 3, 5, 0
+    ws = fslib.walk_step
+    assert ws(10**12, 10**12 + 10**8, 200_000) == H64                      # config 2
+    assert ws(1 << 63, (1 << 63) + 10**9, 1_010_000) == C96                # config 3
+    assert ws(10**6, 2 * 10**6, 2000) == ANY                               # config 1: p < 2^33, generic
+    assert ws(1 << 36, (1 << 36) + 1000, 2000) == H64
+    assert ws((1 << 36) - 1000, (1 << 36) + 1000, 2000) == T64              # straddles 2^36
+    k = 1 << 20
+    assert ws(1 << 40, (1 << 40) + 1, k) == H64                             # p kmax = 2^60
+    assert ws((1 << 42) - 10, (1 << 42) + 1, k) == H64                      # p kmax = 2^62 exactly
+    assert ws((1 << 42) - 10, (1 << 42) + 2, k) == H96                      # just above: 96-bit, half-offset
+    assert ws(10**13, 10**13 + 30_000, (1 << 26) - 1) == H96
+    assert ws(10**13, 10**13 + 30_000, 1 << 26) == L96
+    assert ws(10**13, 10**13 + 30_000, 1 << 28) == ANY                      # k_max >= 2^28: generic
+    assert ws((1 << 63) - 1000, (1 << 63) + 1000, 5000) == ANY              # straddles 2^63
+    assert ws(5, 5, 100) == ANY and ws(10**12, 10**12 + 5, 0) == ANY        # empty ranges

@@ -16,7 +16,7 @@ class FakeCtx:
 
     def tuning(self):
         v = self.t.get("sieve_variant", 3)
-        return {"sieve_variant": v, "sieve_blocks_per_sm": {3: 3, 5: 8, 6: 12}[v]}
+        return {"sieve_variant": v, "sieve_blocks_per_sm": {3: 3, 5: 8}[v]}
 
 
 def test_autotune_picks_fastest_and_caches(tmp_path):
@@ -25,16 +25,16 @@ def test_autotune_picks_fastest_and_caches(tmp_path):
 
     def timer(ctx, cfg, pmin, width, nmin, nmax):
         calls.append(cfg)
-        return 100.0 * cfg["sieve_variant"] - cfg["sieve_blocks_per_sm"]   # best: variant 6 at 12 blocks
+        return 100.0 * cfg["sieve_variant"] - cfg["sieve_blocks_per_sm"]   # best: variant 5 at 8 blocks
 
     ctx = FakeCtx()
     best = tuner.autotune(ctx, 10**12, 100_000, 200_000, gpu_name="X", cache=cache, timer=timer)
-    assert (best["sieve_variant"], best["sieve_blocks_per_sm"]) == (6, 12)
-    assert len(calls) == 6
+    assert (best["sieve_variant"], best["sieve_blocks_per_sm"]) == (5, 8)
+    assert len(calls) == 4
     again = tuner.autotune(ctx, 10**12 + 5, 100_001, 200_003, gpu_name="X", cache=cache, timer=timer)
-    assert len(calls) == 6 and again["sieve_variant"] == 6          # same bucket: cached
+    assert len(calls) == 4 and again["sieve_variant"] == 5          # same bucket: cached
     tuner.autotune(ctx, 10**15, 100_000, 200_000, gpu_name="X", cache=cache, timer=timer)
-    assert len(calls) == 12                                           # new p bucket: tuned again
+    assert len(calls) == 8                                            # new p bucket: tuned again
 
 
 def test_bucket_key_separates_workloads():
@@ -49,7 +49,7 @@ def test_tuned_shape_gives_identical_results(ctx, tmp_path):
     cache = tuner.TuningCache(str(tmp_path / "t.json"))
     best = tuner.autotune(ctx, 10**12, 100_000, 101_000, gpu_name=torch.cuda.get_device_name(0),
                           sample_steps=2e9, cache=cache)
-    assert best["rate"] > 0 and len(best["tried"]) == 6
+    assert best["rate"] > 0 and len(best["tried"]) == 4
     base = ctx.sieve(10**12, 10**12 + 3_000_000, 100_000, 101_000)
     tuner.apply(ctx, best)
     try:
