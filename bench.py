@@ -48,7 +48,7 @@ sys.path.insert(0, ROOT)
 
 WORKLOADS = {
     # name: (pmin, pmax, nmin, nmax, segment width)
-    "config1": (1_000_000, 2_000_000, 1000, 2000, 100_000),
+    "config1": (1_000_000, 2_000_000, 1000, 2000, 1_000_000),      # a step is the whole (small) range
     "config2": (1_000_000_000_000, 1_001_000_000_000, 100_000, 200_000, 100_000_000),
     "config3": (1 << 63, (1 << 63) + 1_000_000_000, 1_000_000, 1_010_000, 100_000_000),
 }
@@ -79,7 +79,8 @@ def reference_setup_products(nmin: int) -> int:
 
 
 # Ceiling microkernels (fs_bench_int_pipe kinds) of each residue step.
-STEP_CEILING_KIND = {4: (5, "half-offset lazy 64-bit step"), 5: (10, "half-offset lazy 96-bit step"),
+STEP_CEILING_KIND = {6: (11, "32-bit half-offset step"), 4: (5, "half-offset lazy 64-bit step"),
+                     5: (10, "half-offset lazy 96-bit step"),
                      1: (6, "lazy 64-bit step"),
                      2: (7, "lazy 96-bit step"), 3: (8, "canonical 96-bit step"),
                      0: (9, "generic Montgomery step")}

@@ -102,6 +102,7 @@ def _declare(L):
         "fs_table_check": (C.c_int, [vp, vp, vp, u32, P64]),
         "fs_plan_check": (C.c_int, [vp, vp, vp, u32, vp, vp, u32, u64, P64]),
         "fs_bench_int_pipe": (C.c_int, [vp, u32, u32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+        "fs_search_pending": (C.c_int, [vp, P64]),
         "fs_walk_step": (C.c_int, [u64, u64, u32]),
         "fs_set_timing": (C.c_int, [vp, C.c_int]),
         "fs_get_stats": (C.c_int, [vp, C.POINTER(Stats)]),
@@ -195,8 +196,8 @@ def setup_plan_chunks(n: int, chunks: int):
 
 def walk_step(plo: int, phi: int, kmax: int) -> int:
     """The residue step the sieve runs for p in [plo, phi), multipliers up to kmax
-    (4 / 5 half-offset lazy 64-bit / 96-bit, 1 lazy 64-bit, 2 lazy 96-bit,
-    3 canonical 96-bit, 0 chosen per candidate)."""
+    (6 / 4 / 5 half-offset 32-bit / lazy 64-bit / lazy 96-bit, 1 lazy 64-bit,
+    2 lazy 96-bit, 3 canonical 96-bit, 0 chosen per candidate)."""
     return int(lib().fs_walk_step(plo, phi, kmax))
 
 
@@ -324,9 +325,13 @@ class Context:
 
     def collect(self, cap, raise_on_flags=True):
         """Wait, then return (hits, raw_sum, primecount, flags, status) accumulated since
-        the last collect; at most `cap` hits are copied."""
+        the last collect; at most `cap` hits are copied (the host buffer is sized to
+        what is pending, not to cap)."""
         L = lib()
         nf, rs, pc, fl = C.c_uint64(0), C.c_uint64(0), C.c_uint64(0), C.c_uint32(0)
+        pend = np.zeros(1, np.uint64)
+        self._chk(L.fs_search_pending(self._h, _p64(pend)), "fs_search_pending")
+        cap = min(cap, int(pend[0]))
         buf = (Factor * max(cap, 1))()
         rc = L.fs_search_collect(self._h, buf, cap, C.byref(nf), C.byref(rs), C.byref(pc), C.byref(fl))
         hits = np.frombuffer(buf, dtype=FACTOR_DTYPE, count=min(nf.value, cap)).copy()

@@ -565,4 +565,76 @@ __device__ __forceinline__ u32 half96_walk8x2(u32& al, u32& ah, u32& bl, u32& bh
     return flag;
 }
 
+// -------------------------- iterate: 32-bit steps, half-offset form (p < 2^31) --
+//
+// For p < 2^31 the residue fits one word: t = r k is a single 32 x 32-bit
+// product, and r' = t - q p < 2^32 needs only the low word, one IMAD.  The
+// quotient takes the 32-bit window z = t >> s, s = max(0, bitlen(p) +
+// bitlen(k_max) - 29), M = floor(2^(32+s) / p): with r < (1 + e) p,
+// z < (1 + e) 2^29 and d < 2^(kb-28) + (1 + e)/8 (no first term when s = 0),
+// fixed point e = 3/7 for k_max < 2^26.  Half-offset form as above: hits are
+// r in {x, x + 1}.  The high word of the residue stays zero.
+struct Half32 {
+    u64 p, x;
+    u32 np, M, sh;            // 2^32 - p, floor(2^(32+s) / p), s
+    u32 x0, x1;               // x and x + 1
+};
+
+__device__ __forceinline__ bool half32_ok(u64 p, u32 kmax) {
+    return p > 2 && p < (1ull << 31) && kmax != 0 && bitlen32(kmax) <= 26;
+}
+
+__device__ __forceinline__ Half32 make_half32(const Prime& c, u32 kmax) {
+    Half32 H;
+    H.p = c.p;
+    H.x = (c.p - 1) >> 1;
+    H.np = (u32)(0ull - c.p);
+    const int s0 = bitlen64(c.p) + bitlen32(kmax) - 29;
+    const int s = s0 > 0 ? s0 : 0;
+    H.sh = (u32)s;
+    H.M = (u32)((1ull << (32 + s)) / c.p);
+    H.x0 = (u32)H.x;
+    H.x1 = (u32)(H.x + 1);
+    return H;
+}
+
+__device__ __forceinline__ u64 half32_step(u64 r, u32 k, const Half32& H) {
+    const u64 t = (u64)(u32)r * (u64)k;
+    const u32 q = __umulhi((u32)(t >> H.sh), H.M);
+    return (u64)(u32)((u32)t + q * H.np);
+}
+__device__ __forceinline__ u64 half32_canon(u64 r, const Half32& H) { return r >= H.p ? r - H.p : r; }
+
+#define FS_H32_MUL(RL, NP, MM, SH, T, T0, T1, Z, Q)                 \
+    "mul.wide.u32 " T ", " RL ", kk;\n\t"                          \
+    "mov.b64 {" T0 ", " T1 "}, " T ";\n\t"                         \
+    "shf.r.clamp.b32 " Z ", " T0 ", " T1 ", " SH ";\n\t"           \
+    "mul.hi.u32 " Q ", " Z ", " MM ";\n\t"                         \
+    "mad.lo.u32 " RL ", " Q ", " NP ", " T0 ";\n\t"
+#define FS_H32_STEP2(J)                                             \
+    "add.u32 kk, %5, " #J ";\n\t"                                   \
+    FS_HF_TEST("%0", "%9", "%10")                                   \
+    FS_HF_TEST("%2", "%14", "%15")                                  \
+    FS_H32_MUL("%0", "%6", "%7", "%8", "TA", "a0", "a1", "az", "aq") \
+    FS_H32_MUL("%2", "%11", "%12", "%13", "TB", "b0", "b1", "bz", "bq")
+
+// Eight 32-bit half-offset steps on two residues (high words untouched, zero).
+__device__ __forceinline__ u32 half32_walk8x2(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const Half32& A,
+                                              const Half32& B) {
+    u32 flag;
+    asm("{\n\t"
+        ".reg .u32 kk, a0, a1, az, aq, b0, b1, bz, bq;\n\t"
+        ".reg .u64 TA, TB;\n\t"
+        ".reg .pred P;\n\t"
+        "setp.ne.u32 P, %5, %5;\n\t"
+        FS_H32_STEP2(0) FS_H32_STEP2(1) FS_H32_STEP2(2) FS_H32_STEP2(3)
+        FS_H32_STEP2(4) FS_H32_STEP2(5) FS_H32_STEP2(6) FS_H32_STEP2(7)
+        "selp.u32 %4, 1, 0, P;\n\t"
+        "}"
+        : "+r"(al), "+r"(ah), "+r"(bl), "+r"(bh), "=r"(flag)
+        : "r"(k1), "r"(A.np), "r"(A.M), "r"(A.sh), "r"(A.x0), "r"(A.x1), "r"(B.np), "r"(B.M), "r"(B.sh),
+          "r"(B.x0), "r"(B.x1));
+    return flag;
+}
+
 }  // namespace fs

@@ -108,6 +108,11 @@ int fs_search_segment(fs_ctx *ctx, uint64_t low, uint64_t high);
  * FS_E_VALIDATION or FS_E_TABLE when the device flagged one. */
 int fs_search_collect(fs_ctx *ctx, fs_factor *out, uint64_t cap, uint64_t *nfactors,
                       uint64_t *raw_sum, uint64_t *primecount, uint32_t *flags);
+/* Wait for the queued segments and report how many factor records the next
+ * fs_search_collect will return (so a caller can size its buffer); clears
+ * nothing.  No counterpart in the reference, whose result buffer has a fixed
+ * size (numresults). */
+int fs_search_pending(fs_ctx *ctx, uint64_t *nfactors);
 /* Convenience: queue segments of width seg_width (0: automatic) over
  * [low, high). */
 int fs_search_range(fs_ctx *ctx, uint64_t low, uint64_t high, uint64_t seg_width);
@@ -245,14 +250,14 @@ int fs_reset_stats(fs_ctx *ctx);
  * arithmetic register-resident at full occupancy (units per second), the
  * ceilings of its roofline: 4 Montgomery products, 5 half-offset lazy
  * steps, 6 lazy 64-bit steps, 7 lazy 96-bit steps, 8 canonical 96-bit
- * steps, 9 generic Montgomery steps, 10 half-offset lazy 96-bit steps.
- * iters in [1, 2^24]. */
+ * steps, 9 generic Montgomery steps, 10 half-offset lazy 96-bit steps,
+ * 11 32-bit half-offset steps.  iters in [1, 2^24]. */
 int fs_bench_int_pipe(fs_ctx *ctx, uint32_t kind, uint32_t iters, double *ops_per_sec, double *ms);
 
 /* The residue step a segment p in [plo, phi) with multipliers up to kmax
- * runs: 4 / 5 half-offset lazy 64-bit / 96-bit, 1 lazy 64-bit, 2 lazy 96-bit,
- * 3 canonical 96-bit, 0 chosen per candidate (mixed, or p < 2^33: generic
- * Montgomery).
+ * runs: 6 / 4 / 5 half-offset 32-bit / lazy 64-bit / lazy 96-bit, 1 lazy
+ * 64-bit, 2 lazy 96-bit, 3 canonical 96-bit, 0 chosen per candidate (mixed,
+ * or 2^31 <= p <= 2^33: generic Montgomery).
  * No counterpart in the reference, whose one step is the Montgomery product. */
 int fs_walk_step(uint64_t plo, uint64_t phi, uint32_t kmax);
 

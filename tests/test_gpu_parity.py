@@ -204,6 +204,8 @@ def test_hit_overflow_is_reported(ctx):
     (10**12, 10**12 + 300_000, 100_000, 100_700),                  # lazy 64-bit step
     ((1 << 36) + 1, (1 << 36) + 300_000, 500_000, 500_300),        # lazy 64-bit step, large multipliers
     ((1 << 33) - 150_000, (1 << 33) + 150_000, 2000, 2900),         # generic / lazy boundary at 2^33
+    ((1 << 31) - 150_000, (1 << 31) + 150_000, 2000, 2900),         # 32-bit / generic boundary at 2^31
+    (10**9, 10**9 + 20_000, 67_108_000, 67_108_800),               # 32-bit step, k_max just below 2^26
     (8 * 10**12, 8 * 10**12 + 300_000, 524_000, 524_400),          # multipliers across 2^19
     ((1 << 36) - 150_000, (1 << 36) + 150_000, 2000, 2900),         # lazy / half-offset boundary at p = 2^36
     ((1 << 40) - 150_000, (1 << 40) + 150_000, 1_047_700, 1 << 20),    # p kmax = 2^60
