@@ -637,4 +637,73 @@ __device__ __forceinline__ u32 half32_walk8x2(u32& al, u32& ah, u32& bl, u32& bh
     return flag;
 }
 
+// ----------- iterate: lazy 64-bit steps, shifted window, half-offset form --
+//
+// 2^31 <= p < 2^36, where the half-offset 64-bit step's window z = t >> 32 is
+// too coarse (2^32/p up to 2) and the 32-bit step's residue does not fit a
+// word: the quotient window is z = t >> s, s = max(0, bitlen(p) +
+// bitlen(k_max) - 29) <= 32, M = floor(2^(32+s) / p), with the same bound as
+// the 96-bit half-offset step (window fixed point 10/7 p) for k_max < 2^25.
+// The step is the half-offset 64-bit step with one funnel shift more.
+__device__ __forceinline__ bool halfmid_ok(u64 p, u32 kmax) {
+    return p >= (1ull << 31) && p < (1ull << 36) && kmax != 0 && bitlen32(kmax) <= 25;
+}
+
+__device__ __forceinline__ Half96 make_halfmid(const Prime& c, u32 kmax) {
+    Half96 H;
+    H.p = c.p;
+    H.x = (c.p - 1) >> 1;
+    const u64 np = 0ull - c.p;
+    H.np0 = (u32)np;
+    H.np1 = (u32)(np >> 32);
+    const int s0 = bitlen64(c.p) + bitlen32(kmax) - 29;
+    const int s = s0 > 0 ? s0 : 0;
+    H.sh = (u32)s;
+    H.M = (u32)((1ull << (32 + s)) / c.p);
+    H.x0 = (u32)H.x;
+    H.x1 = (u32)(H.x + 1);
+    return H;
+}
+
+__device__ __forceinline__ u64 halfmid_step(u64 r, u32 k, const Half96& H) {
+    const u64 t = r * (u64)k;
+    const u32 q = __umulhi((u32)(t >> H.sh), H.M);
+    return t + (u64)q * (((u64)H.np1 << 32) | H.np0);
+}
+
+#define FS_HM_MUL(RL, RH, NP0, NP1, MM, SH, T, R, TL, TH, Z, Q)   \
+    "mul.wide.u32 " T ", " RL ", kk;\n\t"                          \
+    "mov.b64 {" TL ", " TH "}, " T ";\n\t"                         \
+    "mad.lo.u32 " TH ", " RH ", kk, " TH ";\n\t"                   \
+    "shf.r.clamp.b32 " Z ", " TL ", " TH ", " SH ";\n\t"           \
+    "mul.hi.u32 " Q ", " Z ", " MM ";\n\t"                         \
+    "mov.b64 " T ", {" TL ", " TH "};\n\t"                         \
+    "mad.wide.u32 " R ", " Q ", " NP0 ", " T ";\n\t"               \
+    "mov.b64 {" RL ", " RH "}, " R ";\n\t"                         \
+    "mad.lo.u32 " RH ", " Q ", " NP1 ", " RH ";\n\t"
+#define FS_HM_STEP2(J)                                                                   \
+    "add.u32 kk, %5, " #J ";\n\t"                                                        \
+    FS_HF_TEST("%0", "%10", "%11")                                                       \
+    FS_HF_TEST("%2", "%16", "%17")                                                       \
+    FS_HM_MUL("%0", "%1", "%6", "%7", "%8", "%9", "TA", "RA", "aL", "aH", "az", "aq")     \
+    FS_HM_MUL("%2", "%3", "%12", "%13", "%14", "%15", "TB", "RB", "bL", "bH", "bz", "bq")
+
+__device__ __forceinline__ u32 halfmid_walk8x2(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const Half96& A,
+                                               const Half96& B) {
+    u32 flag;
+    asm("{\n\t"
+        ".reg .u32 kk, aL, aH, az, aq, bL, bH, bz, bq;\n\t"
+        ".reg .u64 TA, RA, TB, RB;\n\t"
+        ".reg .pred P;\n\t"
+        "setp.ne.u32 P, %5, %5;\n\t"
+        FS_HM_STEP2(0) FS_HM_STEP2(1) FS_HM_STEP2(2) FS_HM_STEP2(3)
+        FS_HM_STEP2(4) FS_HM_STEP2(5) FS_HM_STEP2(6) FS_HM_STEP2(7)
+        "selp.u32 %4, 1, 0, P;\n\t"
+        "}"
+        : "+r"(al), "+r"(ah), "+r"(bl), "+r"(bh), "=r"(flag)
+        : "r"(k1), "r"(A.np0), "r"(A.np1), "r"(A.M), "r"(A.sh), "r"(A.x0), "r"(A.x1),
+          "r"(B.np0), "r"(B.np1), "r"(B.M), "r"(B.sh), "r"(B.x0), "r"(B.x1));
+    return flag;
+}
+
 }  // namespace fs

@@ -242,7 +242,8 @@ __global__ void __launch_bounds__(256) imad_bench_kernel(u32 iters, u32 kind, u3
 //   kind 9  generic Montgomery steps (mont_mul by kR, k advanced by R), 4 chains
 //   kind 10 half-offset lazy 96-bit steps (half96_walk8x2), 4 chains
 //   kind 11 32-bit half-offset steps (half32_walk8x2), 4 chains
-constexpr u32 kCeilUnits[12] = {0, 0, 0, 0, 8, 32, 32, 32, 32, 4, 32, 32};
+//   kind 12 shifted-window half-offset 64-bit steps (halfmid_walk8x2), 4 chains
+constexpr u32 kCeilUnits[13] = {0, 0, 0, 0, 8, 32, 32, 32, 32, 4, 32, 32, 32};
 
 template <u32 kind>
 __global__ void __launch_bounds__(256) ceiling_kernel(u32 iters, u32 seed, u32* sink) {
@@ -255,6 +256,7 @@ __global__ void __launch_bounds__(256) ceiling_kernel(u32 iters, u32 seed, u32* 
         case 7: base = 1000000000000000ull; break;        // p kmax > 2^62, p < 2^63
         case 10: base = 1000000000000000ull; break;       // p kmax > 2^60, p < 2^63
         case 11: base = 1000000001ull; break;             // p < 2^31
+        case 12: base = (1ull << 33) + 1; break;          // 2^31 <= p < 2^36
         case 8: base = (1ull << 63) + 1; break;           // p >= 2^63
         default: base = (1ull << 63) + 1; break;
     }
@@ -320,6 +322,14 @@ __global__ void __launch_bounds__(256) ceiling_kernel(u32 iters, u32 seed, u32* 
                 acc += half32_walk8x2(l[0], hh[0], l[1], hh[1], k0 + 8 * it, A, B);
                 acc += half32_walk8x2(l[2], hh[2], l[3], hh[3], k0 + 8 * it, C, D);
             }
+        } else if constexpr (kind == 12) {
+            const u32 kmax = k0 + 8 * iters;
+            const Half96 A = make_halfmid(c[0], kmax), B = make_halfmid(c[1], kmax);
+            const Half96 C = make_halfmid(c[2], kmax), D = make_halfmid(c[3], kmax);
+            for (u32 it = 0; it < iters; ++it) {
+                acc += halfmid_walk8x2(l[0], hh[0], l[1], hh[1], k0 + 8 * it, A, B);
+                acc += halfmid_walk8x2(l[2], hh[2], l[3], hh[3], k0 + 8 * it, C, D);
+            }
         } else if constexpr (kind == 10) {
             const u32 kmax = k0 + 8 * iters;
             const Half96 A = make_half96(c[0], kmax), B = make_half96(c[1], kmax);
@@ -379,12 +389,13 @@ cudaError_t launch_imad_bench(u32 iters, u32 kind, u32 seed, u32* sink, int grid
         case 9: ceiling_kernel<9><<<grid, 256, 0, s>>>(iters, seed, sink); break;
         case 10: ceiling_kernel<10><<<grid, 256, 0, s>>>(iters, seed, sink); break;
         case 11: ceiling_kernel<11><<<grid, 256, 0, s>>>(iters, seed, sink); break;
+        case 12: ceiling_kernel<12><<<grid, 256, 0, s>>>(iters, seed, sink); break;
         default: imad_bench_kernel<<<grid, 256, 0, s>>>(iters, kind, seed, sink); break;
     }
     return cudaGetLastError();
 }
 
-double bench_units_per_thread_iter(u32 kind) { return kind < 4 ? 8.0 : (kind < 12 ? kCeilUnits[kind] : 0.0); }
+double bench_units_per_thread_iter(u32 kind) { return kind < 4 ? 8.0 : (kind < 13 ? kCeilUnits[kind] : 0.0); }
 
 int walk_for_range(uint64_t plo, uint64_t phi, uint32_t kmax) {
     if (phi <= plo || kmax == 0) return WALK_ANY;
@@ -392,6 +403,8 @@ int walk_for_range(uint64_t plo, uint64_t phi, uint32_t kmax) {
     const int kb = 32 - __builtin_clz(kmax);
     // the 32-bit half-offset step needs 2 < p < 2^31 and kmax < 2^26 (half32_ok)
     if (plo > 2 && pmax < (1ull << 31) && kb <= 26) return WALK_H32;
+    // the shifted-window half-offset step needs 2^31 <= p < 2^36 and kmax < 2^25 (halfmid_ok)
+    if (plo >= (1ull << 31) && pmax < (1ull << 36) && kb <= 25) return WALK_HM;
     // the half-offset lazy step needs p >= 2^36 and p kmax <= 2^62 (half_ok)
     if (plo >= (1ull << 36) && pmax <= ((1ull << 62) / kmax)) return WALK_H64;
     // the lazy 64-bit step needs p > 2^33 and p kmax <= 2^62 (lazy_ok)

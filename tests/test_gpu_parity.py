@@ -204,7 +204,9 @@ def test_hit_overflow_is_reported(ctx):
     (10**12, 10**12 + 300_000, 100_000, 100_700),                  # lazy 64-bit step
     ((1 << 36) + 1, (1 << 36) + 300_000, 500_000, 500_300),        # lazy 64-bit step, large multipliers
     ((1 << 33) - 150_000, (1 << 33) + 150_000, 2000, 2900),         # generic / lazy boundary at 2^33
-    ((1 << 31) - 150_000, (1 << 31) + 150_000, 2000, 2900),         # 32-bit / generic boundary at 2^31
+    ((1 << 31) - 150_000, (1 << 31) + 150_000, 2000, 2900),         # 32-bit / shifted-window boundary at 2^31
+    ((1 << 34) + 1, (1 << 34) + 300_001, 20_000, 20_900),          # shifted-window 64-bit step
+    ((1 << 32) + 1, (1 << 32) + 20_001, (1 << 25) - 700, (1 << 25) - 1),  # shifted window, k_max just below 2^25
     (10**9, 10**9 + 20_000, 67_108_000, 67_108_800),               # 32-bit step, k_max just below 2^26
     (8 * 10**12, 8 * 10**12 + 300_000, 524_000, 524_400),          # multipliers across 2^19
     ((1 << 36) - 150_000, (1 << 36) + 150_000, 2000, 2900),         # lazy / half-offset boundary at p = 2^36

@@ -132,17 +132,19 @@ def test_context_needs_a_device(fslib):
 
 def test_walk_step_selection_boundaries(fslib):
     """The launch-wide step the host proves valid for a p-segment (fs_walk_step)."""
-    H64, T64, L96, C96, H96, H32, ANY = 4, 1, 2, 3, 5, 6, 0
+    H64, T64, L96, C96, H96, H32, HM, ANY = 4, 1, 2, 3, 5, 6, 7, 0
     ws = fslib.walk_step
     assert ws(10**12, 10**12 + 10**8, 200_000) == H64                      # config 2
     assert ws(1 << 63, (1 << 63) + 10**9, 1_010_000) == C96                # config 3
     assert ws(10**6, 2 * 10**6, 2000) == H32                               # config 1: p < 2^31
     assert ws(127, 100_000, 1_000_000) == H32                              # self test 3 (p <= nmax)
     assert ws((1 << 31) - 1000, (1 << 31) + 1000, 2000) == ANY              # straddles 2^31
-    assert ws((1 << 32) + 1, (1 << 32) + 1000, 2000) == ANY                 # 2^31 < p <= 2^33: generic
+    assert ws((1 << 32) + 1, (1 << 32) + 1000, 2000) == HM                  # 2^31 <= p < 2^36: shifted window
+    assert ws((1 << 32) + 1, (1 << 32) + 1000, 1 << 25) == ANY              # ... with k_max >= 2^25: generic
     assert ws(10**6, 2 * 10**6, 1 << 26) == ANY                             # k_max >= 2^26 at small p
     assert ws(1 << 36, (1 << 36) + 1000, 2000) == H64
-    assert ws((1 << 36) - 1000, (1 << 36) + 1000, 2000) == T64              # straddles 2^36
+    assert ws((1 << 36) - 1000, (1 << 36) + 1000, 2000) == T64              # straddles 2^36: the step valid on both sides
+    assert ws((1 << 35) + 1, (1 << 35) + 1000, 1 << 25) == T64              # 2^33 < p < 2^36, k_max >= 2^25
     k = 1 << 20
     assert ws(1 << 40, (1 << 40) + 1, k) == H64                             # p kmax = 2^60
     assert ws((1 << 42) - 10, (1 << 42) + 1, k) == H64                      # p kmax = 2^62 exactly
