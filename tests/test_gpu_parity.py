@@ -327,3 +327,39 @@ def test_known_large_factors_are_found(ctx, orc, variant, p, n, c):
         ctx.set_tuning()
     assert (r.primecount, r.raw_sum, r.checksum) == (want["primecount"], want["raw_sum"], want["checksum"])
     assert [(int(q), int(nc)) for q, nc in zip(r.factors["p"], r.factors["nc"])] == want["factors"]
+
+
+def _random_cases(n, seed):
+    import math
+    import random
+    rng = random.Random(seed)
+    out = []
+    for _ in range(n):
+        lo = int(math.exp(rng.uniform(math.log(1 << 7), math.log((1 << 64) - 2_000_000))))
+        width = rng.randrange(20_000, 120_000)
+        nmin = int(math.exp(rng.uniform(math.log(34), math.log(300_000))))
+        out.append((max(lo, nmin), max(lo, nmin) + width, nmin, nmin + rng.randrange(1, 6000)))
+    return out
+
+
+@pytest.mark.parametrize("lo,hi,nmin,nmax", _random_cases(64, 20261204))
+def test_random_ranges_match_oracle(ctx, orc, lo, hi, nmin, nmax):
+    """Seeded random p-ranges (log-uniform over [2^7, 2^64)) and n-ranges (nmin
+    log-uniform over [34, 3e5)): the whole search (launch-wide step, four
+    candidates per thread) and the stage-level path (a step chosen per
+    candidate, two per thread) both equal the oracle bit for bit."""
+    import factsieve_gb300 as fs
+    want = orc.run(lo, hi, nmin, nmax)
+    assert want["status"] == 0
+    r = ctx.sieve(lo, hi, nmin, nmax)
+    assert (r.primecount, r.raw_sum, r.checksum, r.factorcount) == \
+        (want["primecount"], want["raw_sum"], want["checksum"], want["factorcount"])
+    cap = fs.candidate_capacity(lo, hi)
+    cand, res, hits, ctr = _dev_buffers(cap)
+    ctx.getsegprimes(lo, hi, cand.data_ptr(), cap, ctr.data_ptr())
+    ctx.setup(cand.data_ptr(), cap, ctr.data_ptr(), nmin, res.data_ptr())
+    ctx.iterate(cand.data_ptr(), cap, ctr.data_ptr(), res.data_ptr(), nmin, nmax, hits.data_ptr(), 1 << 16)
+    ctx.check(cand.data_ptr(), cap, ctr.data_ptr(), res.data_ptr(), nmax)
+    ctx.synchronize()
+    cs = _counters(ctr)
+    assert (int(cs["raw_sum"]), int(cs["flags"]), int(cs["nhits"])) == (want["raw_sum"], 0, want["nhits"])
