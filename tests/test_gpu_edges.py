@@ -123,3 +123,23 @@ def test_ceiling_kernels_report_rates(ctx):
         ctx.bench_int_pipe(13, 200)
     with pytest.raises(fs.FSError):
         ctx.bench_int_pipe(5, 0)
+
+
+def test_pending_count_sizes_collect(ctx, orc):
+    """fs_search_pending reports, without clearing, the records the next collect
+    returns; collect then copies exactly those."""
+    import numpy as np
+    import factsieve_gb300 as fs
+    lo, hi, nmin, nmax = 127, 100_000, 127, 2_000
+    want = orc.run(lo, hi, nmin, nmax)
+    ctx.begin(lo, hi, nmin, nmax)
+    ctx.segment(lo, hi)
+    pend = np.zeros(1, np.uint64)
+    assert fs.lib().fs_search_pending(ctx.handle, fs._p64(pend)) == 0
+    assert int(pend[0]) == want["nhits"] > 0
+    assert fs.lib().fs_search_pending(ctx.handle, fs._p64(pend)) == 0      # unchanged: nothing cleared
+    assert int(pend[0]) == want["nhits"]
+    hits, raw, pc, flags, rc = ctx.collect(1 << 20)
+    assert (len(hits), raw, pc, rc) == (want["nhits"], want["raw_sum"], want["primecount"], 0)
+    assert fs.lib().fs_search_pending(ctx.handle, fs._p64(pend)) == 0
+    assert int(pend[0]) == 0                                                # collect cleared them
