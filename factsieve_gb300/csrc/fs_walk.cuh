@@ -119,8 +119,10 @@ __device__ __forceinline__ void plan_product2(const Prime& a, const Prime& b, co
     xb = y;
 }
 
-// The same for four candidates: four independent product chains per table
-// load, for the four-candidate sieve kernel.
+// The same for four candidates, each product split over two chains (even
+// and odd words of a layer, the odd chain started at R = one so that joining
+// them with one more Montgomery product leaves the deficit unchanged): eight
+// independent chains per thread and one table load per four candidates.
 __device__ __forceinline__ void plan_product4(const Prime (&c)[4], const u64* __restrict__ words,
                                               const Layer* __restrict__ layers, u32 lb, u32 le, u64 (&x)[4]) {
 #pragma unroll
@@ -141,12 +143,20 @@ __device__ __forceinline__ void plan_product4(const Prime (&c)[4], const u64* __
 #pragma unroll
             for (int h = 0; h < 4; ++h) x[h] = mont_mul(x[h], w, c[h].p, c[h].pinv);
         }
-        for (; i + 2 <= L.end; i += 2) {
-            const ulonglong2 w2 = __ldg(reinterpret_cast<const ulonglong2*>(words + i));
+        if (i + 2 <= L.end) {
+            u64 y[4];
 #pragma unroll
-            for (int h = 0; h < 4; ++h) x[h] = mont_mul(x[h], w2.x, c[h].p, c[h].pinv);
+            for (int h = 0; h < 4; ++h) y[h] = c[h].one;
+            for (; i + 2 <= L.end; i += 2) {
+                const ulonglong2 w2 = __ldg(reinterpret_cast<const ulonglong2*>(words + i));
 #pragma unroll
-            for (int h = 0; h < 4; ++h) x[h] = mont_mul(x[h], w2.y, c[h].p, c[h].pinv);
+                for (int h = 0; h < 4; ++h) {
+                    x[h] = mont_mul(x[h], w2.x, c[h].p, c[h].pinv);
+                    y[h] = mont_mul(y[h], w2.y, c[h].p, c[h].pinv);
+                }
+            }
+#pragma unroll
+            for (int h = 0; h < 4; ++h) x[h] = mont_mul(x[h], y[h], c[h].p, c[h].pinv);
         }
         if (i < L.end) {
             const u64 w = __ldg(words + i);
