@@ -81,7 +81,7 @@ def reference_setup_products(nmin: int) -> int:
 # Ceiling microkernels (fs_bench_int_pipe kinds) of each residue step.
 STEP_CEILING_KIND = {6: (11, "32-bit half-offset step"), 7: (12, "shifted-window half-offset 64-bit step"),
                      4: (5, "half-offset lazy 64-bit step"),
-                     5: (10, "half-offset lazy 96-bit step"),
+                     5: (10, "half-offset lazy 96-bit step"), 8: (13, "half-offset canonical 96-bit step"),
                      1: (6, "lazy 64-bit step"),
                      2: (7, "lazy 96-bit step"), 3: (8, "canonical 96-bit step"),
                      0: (9, "generic Montgomery step")}

@@ -196,9 +196,9 @@ def setup_plan_chunks(n: int, chunks: int):
 
 def walk_step(plo: int, phi: int, kmax: int) -> int:
     """The residue step the sieve runs for p in [plo, phi), multipliers up to kmax
-    (6 / 7 / 4 / 5 half-offset 32-bit / shifted-window 64-bit / lazy 64-bit /
-    lazy 96-bit, 1 lazy 64-bit, 2 lazy 96-bit, 3 canonical 96-bit, 0 chosen per
-    candidate)."""
+    (6 / 7 / 4 / 5 / 8 half-offset 32-bit / shifted-window 64-bit / lazy 64-bit /
+    lazy 96-bit / canonical 96-bit, 1 lazy 64-bit, 2 lazy 96-bit, 3 canonical
+    96-bit, 0 chosen per candidate)."""
     return int(lib().fs_walk_step(plo, phi, kmax))
 
 

@@ -706,4 +706,107 @@ __device__ __forceinline__ u32 halfmid_walk8x2(u32& al, u32& ah, u32& bl, u32& b
     return flag;
 }
 
+// ------------------- iterate: 96-bit steps for p >= 2^63, half-offset form --
+//
+// For p >= 2^63 a residue of the lazy window needs 65 bits.  Inside one
+// eight-step PTX block the 65th bit is kept in a register (t gains W k 2^64
+// from it, one mad.lo) and the window fold of the canonical step is skipped;
+// the residue is folded once, at the end of the block, so every residue
+// that leaves the block is canonical.  With the window z = t >> s, s =
+// 64 + bitlen(k_max) - 29, the lazy residue stays below (10/7) p for k_max <
+// 2^26 (the bound of the other 96-bit half-offset step), and in half-offset
+// form (x = (p - 1)/2) a hit is r = x or x + 1 with the 65th bit clear.
+struct Canon96H {
+    u64 p, x;
+    u32 p0, p1, M, sh;        // p (two words), floor(2^(32+s) / p), s - 32
+    u32 x0, x1;               // low words of x and x + 1
+};
+
+__device__ __forceinline__ bool canon96h_ok(u64 p, u32 kmax) {
+    return (p >> 63) != 0 && kmax != 0 && bitlen32(kmax) <= 26;
+}
+
+__device__ __forceinline__ Canon96H make_canon96h(const Prime& c, u32 kmax) {
+    Canon96H C;
+    C.p = c.p;
+    C.x = (c.p - 1) >> 1;
+    C.p0 = (u32)c.p;
+    C.p1 = (u32)(c.p >> 32);
+    const int s = 64 + bitlen32(kmax) - 29;
+    C.sh = (u32)(s - 32);
+    C.M = recip_pow2(c.p, 32 + s);
+    C.x0 = (u32)C.x;
+    C.x1 = (u32)(C.x + 1);
+    return C;
+}
+
+// One step with the fold (canonical in and out): the replay and tail steps.
+__device__ __forceinline__ u64 canon96h_step(u64 r, u32 k, const Canon96H& C) {
+    const u64 lo = r * (u64)k, hi = __umul64hi(r, (u64)k);
+    const u32 q = __umulhi(top_bits(lo, hi, C.sh), C.M);
+    const u64 qlo = (u64)q * C.p, qhi = __umul64hi((u64)q, C.p);
+    const u64 rl = lo - qlo;
+    const u64 r2 = hi - qhi - (lo < qlo ? 1ull : 0ull);
+    return (r2 || rl >= C.p) ? rl - C.p : rl;
+}
+
+#define FS_C96H_MUL(RL, RH, W, P0, P1, MM, SH, T, U, A, B, CC, T0, C, T1, T2, Z, Q, X0, X1, Y1, Y2) \
+    "mul.wide.u32 " T ", " RL ", kk;\n\t"                                        \
+    "mov.b64 {" T0 ", " C "}, " T ";\n\t"                                        \
+    "mov.b64 " CC ", {" C ", zr};\n\t"                                           \
+    "mad.wide.u32 " U ", " RH ", kk, " CC ";\n\t"                                \
+    "mov.b64 {" T1 ", " T2 "}, " U ";\n\t"                                       \
+    "mad.lo.u32 " T2 ", " W ", kk, " T2 ";\n\t"                                  \
+    "shf.r.clamp.b32 " Z ", " T1 ", " T2 ", " SH ";\n\t"                         \
+    "mul.hi.u32 " Q ", " Z ", " MM ";\n\t"                                       \
+    "mul.wide.u32 " A ", " Q ", " P0 ";\n\t"                                     \
+    "mov.b64 {" X0 ", " X1 "}, " A ";\n\t"                                       \
+    "mov.b64 " CC ", {" X1 ", zr};\n\t"                                          \
+    "mad.wide.u32 " B ", " Q ", " P1 ", " CC ";\n\t"                             \
+    "mov.b64 {" Y1 ", " Y2 "}, " B ";\n\t"                                       \
+    "sub.cc.u32 " RL ", " T0 ", " X0 ";\n\t"                                     \
+    "subc.cc.u32 " RH ", " T1 ", " Y1 ";\n\t"                                    \
+    "subc.u32 " W ", " T2 ", " Y2 ";\n\t"
+#define FS_C96H_STEP2(J)                                                                                  \
+    "add.u32 kk, %5, " #J ";\n\t"                                                                         \
+    FS_HF_TEST("%0", "%10", "%11")                                                                        \
+    FS_HF_TEST("%2", "%16", "%17")                                                                        \
+    FS_C96H_MUL("%0", "%1", "aw", "%6", "%7", "%8", "%9", "TA", "UA", "AA", "BA", "CA", "a0", "ac", "a1", "a2", \
+                "az", "aq", "ax0", "ax1", "ay1", "ay2")                                                   \
+    FS_C96H_MUL("%2", "%3", "bw", "%12", "%13", "%14", "%15", "TB", "UB", "AB", "BB", "CB", "b0", "bc", "b1",   \
+                "b2", "bz", "bq", "bx0", "bx1", "by1", "by2")
+// fold a 65-bit residue below 2p back into [0, p)
+#define FS_C96H_FOLD(RL, RH, W, R64, PP, P0, P1, G)          \
+    "mov.b64 " R64 ", {" RL ", " RH "};\n\t"                  \
+    "setp.ge.u64 " G ", " R64 ", " PP ";\n\t"                 \
+    "setp.ne.or.u32 " G ", " W ", 0, " G ";\n\t"              \
+    "@" G " sub.cc.u32 " RL ", " RL ", " P0 ";\n\t"           \
+    "@" G " subc.u32 " RH ", " RH ", " P1 ";\n\t"
+
+__device__ __forceinline__ u32 canon96h_walk8x2(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const Canon96H& A,
+                                                const Canon96H& B) {
+    u32 flag;
+    asm("{\n\t"
+        ".reg .u32 kk, zr, a0, ac, a1, a2, az, aq, ax0, ax1, ay1, ay2, aw;\n\t"
+        ".reg .u32 b0, bc, b1, b2, bz, bq, bx0, bx1, by1, by2, bw;\n\t"
+        ".reg .u64 TA, UA, AA, BA, CA, RA, PA, TB, UB, AB, BB, CB, RB, PB;\n\t"
+        ".reg .pred P, GA, GB;\n\t"
+        "mov.u32 zr, 0;\n\t"
+        "mov.u32 aw, 0;\n\t"
+        "mov.u32 bw, 0;\n\t"
+        "mov.b64 PA, {%6, %7};\n\t"
+        "mov.b64 PB, {%12, %13};\n\t"
+        "setp.ne.u32 P, %5, %5;\n\t"
+        FS_C96H_STEP2(0) FS_C96H_STEP2(1) FS_C96H_STEP2(2) FS_C96H_STEP2(3)
+        FS_C96H_STEP2(4) FS_C96H_STEP2(5) FS_C96H_STEP2(6) FS_C96H_STEP2(7)
+        FS_C96H_FOLD("%0", "%1", "aw", "RA", "PA", "%6", "%7", "GA")
+        FS_C96H_FOLD("%2", "%3", "bw", "RB", "PB", "%12", "%13", "GB")
+        "selp.u32 %4, 1, 0, P;\n\t"
+        "}"
+        : "+r"(al), "+r"(ah), "+r"(bl), "+r"(bh), "=r"(flag)
+        : "r"(k1), "r"(A.p0), "r"(A.p1), "r"(A.M), "r"(A.sh), "r"(A.x0), "r"(A.x1),
+          "r"(B.p0), "r"(B.p1), "r"(B.M), "r"(B.sh), "r"(B.x0), "r"(B.x1));
+    return flag;
+}
+
 }  // namespace fs

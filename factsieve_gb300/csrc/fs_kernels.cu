@@ -243,7 +243,8 @@ __global__ void __launch_bounds__(256) imad_bench_kernel(u32 iters, u32 kind, u3
 //   kind 10 half-offset lazy 96-bit steps (half96_walk8x2), 4 chains
 //   kind 11 32-bit half-offset steps (half32_walk8x2), 4 chains
 //   kind 12 shifted-window half-offset 64-bit steps (halfmid_walk8x2), 4 chains
-constexpr u32 kCeilUnits[13] = {0, 0, 0, 0, 8, 32, 32, 32, 32, 4, 32, 32, 32};
+//   kind 13 half-offset canonical 96-bit steps (canon96h_walk8x2), 4 chains
+constexpr u32 kCeilUnits[14] = {0, 0, 0, 0, 8, 32, 32, 32, 32, 4, 32, 32, 32, 32};
 
 template <u32 kind>
 __global__ void __launch_bounds__(256) ceiling_kernel(u32 iters, u32 seed, u32* sink) {
@@ -257,6 +258,7 @@ __global__ void __launch_bounds__(256) ceiling_kernel(u32 iters, u32 seed, u32* 
         case 10: base = 1000000000000000ull; break;       // p kmax > 2^60, p < 2^63
         case 11: base = 1000000001ull; break;             // p < 2^31
         case 12: base = (1ull << 33) + 1; break;          // 2^31 <= p < 2^36
+        case 13: base = (1ull << 63) + 1; break;          // p >= 2^63
         case 8: base = (1ull << 63) + 1; break;           // p >= 2^63
         default: base = (1ull << 63) + 1; break;
     }
@@ -330,6 +332,14 @@ __global__ void __launch_bounds__(256) ceiling_kernel(u32 iters, u32 seed, u32* 
                 acc += halfmid_walk8x2(l[0], hh[0], l[1], hh[1], k0 + 8 * it, A, B);
                 acc += halfmid_walk8x2(l[2], hh[2], l[3], hh[3], k0 + 8 * it, C, D);
             }
+        } else if constexpr (kind == 13) {
+            const u32 kmax = k0 + 8 * iters;
+            const Canon96H A = make_canon96h(c[0], kmax), B = make_canon96h(c[1], kmax);
+            const Canon96H C = make_canon96h(c[2], kmax), D = make_canon96h(c[3], kmax);
+            for (u32 it = 0; it < iters; ++it) {
+                acc += canon96h_walk8x2(l[0], hh[0], l[1], hh[1], k0 + 8 * it, A, B);
+                acc += canon96h_walk8x2(l[2], hh[2], l[3], hh[3], k0 + 8 * it, C, D);
+            }
         } else if constexpr (kind == 10) {
             const u32 kmax = k0 + 8 * iters;
             const Half96 A = make_half96(c[0], kmax), B = make_half96(c[1], kmax);
@@ -390,12 +400,13 @@ cudaError_t launch_imad_bench(u32 iters, u32 kind, u32 seed, u32* sink, int grid
         case 10: ceiling_kernel<10><<<grid, 256, 0, s>>>(iters, seed, sink); break;
         case 11: ceiling_kernel<11><<<grid, 256, 0, s>>>(iters, seed, sink); break;
         case 12: ceiling_kernel<12><<<grid, 256, 0, s>>>(iters, seed, sink); break;
+        case 13: ceiling_kernel<13><<<grid, 256, 0, s>>>(iters, seed, sink); break;
         default: imad_bench_kernel<<<grid, 256, 0, s>>>(iters, kind, seed, sink); break;
     }
     return cudaGetLastError();
 }
 
-double bench_units_per_thread_iter(u32 kind) { return kind < 4 ? 8.0 : (kind < 13 ? kCeilUnits[kind] : 0.0); }
+double bench_units_per_thread_iter(u32 kind) { return kind < 4 ? 8.0 : (kind < 14 ? kCeilUnits[kind] : 0.0); }
 
 int walk_for_range(uint64_t plo, uint64_t phi, uint32_t kmax) {
     if (phi <= plo || kmax == 0) return WALK_ANY;
@@ -414,6 +425,8 @@ int walk_for_range(uint64_t plo, uint64_t phi, uint32_t kmax) {
     if (kb <= 26 && plo > (1ull << 33) && (pmax >> 63) == 0 && (64 - __builtin_clzll(plo)) + kb >= 61)
         return WALK_H96;
     if (kb <= 28 && plo > (1ull << 33) && (pmax >> 63) == 0) return WALK_L96;
+    // the half-offset canonical 96-bit step needs p >= 2^63 and kmax < 2^26 (canon96h_ok)
+    if (kb <= 26 && (plo >> 63) != 0) return WALK_C96H;
     if (kb <= 28 && (plo >> 63) != 0) return WALK_C96;
     return WALK_ANY;
 }

@@ -25,6 +25,7 @@ cudaError_t launch_sieve_quad(const SieveArgs& a, int setup, bool final_chunk, i
         case WALK_H96: launch_sieve_w<2, WALK_H96, 4>(a, setup, final_chunk, grid, s); break;
         case WALK_H32: launch_sieve_w<2, WALK_H32, 4>(a, setup, final_chunk, grid, s); break;
         case WALK_HM: launch_sieve_w<2, WALK_HM, 4>(a, setup, final_chunk, grid, s); break;
+        case WALK_C96H: launch_sieve_w<2, WALK_C96H, 4>(a, setup, final_chunk, grid, s); break;
         case WALK_T64: launch_sieve_w<2, WALK_T64, 4>(a, setup, final_chunk, grid, s); break;
         case WALK_L96: launch_sieve_w<2, WALK_L96, 4>(a, setup, final_chunk, grid, s); break;
         case WALK_C96: launch_sieve_w<2, WALK_C96, 4>(a, setup, final_chunk, grid, s); break;

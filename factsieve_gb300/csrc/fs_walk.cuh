@@ -262,6 +262,18 @@ struct RegHM {
     }
     static __device__ __forceinline__ int hit(u64 c, const K& X) { return c == X.x ? -1 : (c == X.x + 1 ? 1 : 0); }
 };
+struct RegC96H {
+    using K = Canon96H;
+    static __device__ __forceinline__ K make(const Prime& c, u32 kmax) { return make_canon96h(c, kmax); }
+    static __device__ __forceinline__ u32 block(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const K& A, const K& B) {
+        return canon96h_walk8x2(al, ah, bl, bh, k1, A, B);
+    }
+    static __device__ __forceinline__ u64 step(u64 r, u32 k, const K& X) { return canon96h_step(r, k, X); }
+    static __device__ __forceinline__ u64 canon(u64 r, const K&) { return r; }
+    static __device__ __forceinline__ u64 enter(u64 r, const Prime& c, const K& X) { return half_enter(r, c, X.x); }
+    static __device__ __forceinline__ u64 leave(u64 r, const Prime& c, const K&) { return half_leave(r, c); }
+    static __device__ __forceinline__ int hit(u64 c, const K& X) { return c == X.x ? -1 : (c == X.x + 1 ? 1 : 0); }
+};
 struct RegH96 {
     using K = Half96;
     static __device__ __forceinline__ K make(const Prime& c, u32 kmax) { return make_half96(c, kmax); }
@@ -348,12 +360,14 @@ __device__ __forceinline__ u64 walk_generic(u64 r, const Prime& c, u32 nstart, u
     return r;
 }
 
-// Walk regime of one candidate for multipliers up to kmax: 6 / 7 / 4 / 5
-// 32-bit / shifted-window 64-bit / lazy 64-bit / 96-bit in half-offset form,
-// 1 lazy 64-bit, 2 lazy 96-bit, 3 canonical 96-bit, 0 generic Montgomery.
+// Walk regime of one candidate for multipliers up to kmax: 6 / 7 / 4 / 5 / 8
+// 32-bit / shifted-window 64-bit / lazy 64-bit / lazy 96-bit / canonical
+// 96-bit in half-offset form, 1 lazy 64-bit, 2 lazy 96-bit, 3 canonical
+// 96-bit, 0 generic Montgomery.
 __device__ __forceinline__ int walk_regime(u64 p, u32 kmax) {
     if (half32_ok(p, kmax)) return 6;
     if (halfmid_ok(p, kmax)) return 7;
+    if (canon96h_ok(p, kmax)) return 8;
     if (half_ok(p, kmax)) return 4;
     if (lazy_ok(p, kmax)) return 1;
     if (half96_ok(p, kmax)) return 5;
@@ -372,6 +386,7 @@ __device__ __forceinline__ void walk_one(u64& r, const Prime& c, int reg, u32 ns
         case 5: walk_reg_pair<RegH96>(r, dup, c, c, false, nstart, nend, o); break;
         case 6: walk_reg_pair<RegH32>(r, dup, c, c, false, nstart, nend, o); break;
         case 7: walk_reg_pair<RegHM>(r, dup, c, c, false, nstart, nend, o); break;
+        case 8: walk_reg_pair<RegC96H>(r, dup, c, c, false, nstart, nend, o); break;
         default: r = walk_generic(r, c, nstart, nend, o); break;
     }
 }
@@ -397,6 +412,7 @@ __device__ __forceinline__ void walk_pair(u64& ra, u64& rb, const Prime& a, cons
             case 5: walk_reg_pair<RegH96>(ra, rb, a, b, real_b, nstart, nend, o); return;
             case 6: walk_reg_pair<RegH32>(ra, rb, a, b, real_b, nstart, nend, o); return;
             case 7: walk_reg_pair<RegHM>(ra, rb, a, b, real_b, nstart, nend, o); return;
+            case 8: walk_reg_pair<RegC96H>(ra, rb, a, b, real_b, nstart, nend, o); return;
             default: walk_reg_pair<RegC96>(ra, rb, a, b, real_b, nstart, nend, o); return;
         }
     }
@@ -412,6 +428,7 @@ __device__ __forceinline__ void walk_pair_as(u64& ra, u64& rb, const Prime& a, c
     else if (WALK == WALK_H96) walk_reg_pair<RegH96>(ra, rb, a, b, real_b, nstart, nend, o);
     else if (WALK == WALK_H32) walk_reg_pair<RegH32>(ra, rb, a, b, real_b, nstart, nend, o);
     else if (WALK == WALK_HM) walk_reg_pair<RegHM>(ra, rb, a, b, real_b, nstart, nend, o);
+    else if (WALK == WALK_C96H) walk_reg_pair<RegC96H>(ra, rb, a, b, real_b, nstart, nend, o);
     else if (WALK == WALK_T64) walk_reg_pair<RegT64>(ra, rb, a, b, real_b, nstart, nend, o);
     else if (WALK == WALK_L96) walk_reg_pair<RegL96>(ra, rb, a, b, real_b, nstart, nend, o);
     else if (WALK == WALK_C96) walk_reg_pair<RegC96>(ra, rb, a, b, real_b, nstart, nend, o);
@@ -490,6 +507,7 @@ __device__ __forceinline__ void walk_quad_as(u64 (&r)[4], Prime (&c)[4], u32 nre
     else if (WALK == WALK_H96) walk_reg4<RegH96>(r, c, nreal, nstart, nend, o);
     else if (WALK == WALK_H32) walk_reg4<RegH32>(r, c, nreal, nstart, nend, o);
     else if (WALK == WALK_HM) walk_reg4<RegHM>(r, c, nreal, nstart, nend, o);
+    else if (WALK == WALK_C96H) walk_reg4<RegC96H>(r, c, nreal, nstart, nend, o);
     else if (WALK == WALK_T64) walk_reg4<RegT64>(r, c, nreal, nstart, nend, o);
     else if (WALK == WALK_L96) walk_reg4<RegL96>(r, c, nreal, nstart, nend, o);
     else if (WALK == WALK_C96) walk_reg4<RegC96>(r, c, nreal, nstart, nend, o);
@@ -508,6 +526,7 @@ __device__ __forceinline__ void walk_quad_rt(int walk, u64 (&r)[4], Prime (&c)[4
         case WALK_H96: walk_quad_as<WALK_H96>(r, c, nreal, nstart, nend, o); break;
         case WALK_H32: walk_quad_as<WALK_H32>(r, c, nreal, nstart, nend, o); break;
         case WALK_HM: walk_quad_as<WALK_HM>(r, c, nreal, nstart, nend, o); break;
+        case WALK_C96H: walk_quad_as<WALK_C96H>(r, c, nreal, nstart, nend, o); break;
         case WALK_T64: walk_quad_as<WALK_T64>(r, c, nreal, nstart, nend, o); break;
         case WALK_L96: walk_quad_as<WALK_L96>(r, c, nreal, nstart, nend, o); break;
         case WALK_C96: walk_quad_as<WALK_C96>(r, c, nreal, nstart, nend, o); break;

@@ -198,7 +198,9 @@ def test_hit_overflow_is_reported(ctx):
     (10**15, 10**15 + 300_000, 100_000, 100_700),                  # half-offset 96-bit step (p < 2^63, p k > 2^62)
     (10**13, 10**13 + 30_000, 67_109_000, 67_109_700),             # lazy 96-bit step (k_max >= 2^26)
     (10**13, 10**13 + 30_000, 67_108_000, 67_108_800),             # half-offset 96-bit step, k_max just below 2^26
-    ((1 << 63) + 1, (1 << 63) + 300_000, 5_000, 5_700),             # canonical 96-bit step (p >= 2^63)
+    ((1 << 63) + 1, (1 << 63) + 300_000, 5_000, 5_700),             # half-offset canonical 96-bit step (p >= 2^63)
+    ((1 << 63) + 1, (1 << 63) + 10_001, (1 << 26) + 100, (1 << 26) + 700),  # canonical 96-bit step (k_max >= 2^26)
+    ((1 << 64) - 20_000, (1 << 64) - 1, (1 << 26) - 800, (1 << 26) - 1),    # half-offset at p near 2^64, k_max near 2^26
     ((1 << 64) - 400_000, (1 << 64) - 1, 1_000, 1_333),              # canonical 96-bit step near 2^64
     (4 * 10**12, 4 * 10**12 + 200_000, 1_000_000, 1_000_300),      # across the 64/96-bit boundary
     (10**12, 10**12 + 300_000, 100_000, 100_700),                  # lazy 64-bit step

@@ -132,10 +132,11 @@ def test_context_needs_a_device(fslib):
 
 def test_walk_step_selection_boundaries(fslib):
     """The launch-wide step the host proves valid for a p-segment (fs_walk_step)."""
-    H64, T64, L96, C96, H96, H32, HM, ANY = 4, 1, 2, 3, 5, 6, 7, 0
+    H64, T64, L96, C96, H96, H32, HM, C96H, ANY = 4, 1, 2, 3, 5, 6, 7, 8, 0
     ws = fslib.walk_step
     assert ws(10**12, 10**12 + 10**8, 200_000) == H64                      # config 2
-    assert ws(1 << 63, (1 << 63) + 10**9, 1_010_000) == C96                # config 3
+    assert ws(1 << 63, (1 << 63) + 10**9, 1_010_000) == C96H               # config 3
+    assert ws(1 << 63, (1 << 63) + 10**9, 1 << 26) == C96                   # k_max >= 2^26 at p >= 2^63
     assert ws(10**6, 2 * 10**6, 2000) == H32                               # config 1: p < 2^31
     assert ws(127, 100_000, 1_000_000) == H32                              # self test 3 (p <= nmax)
     assert ws((1 << 31) - 1000, (1 << 31) + 1000, 2000) == ANY              # straddles 2^31
