@@ -103,7 +103,7 @@ def roofline(ctx, fs, wl, ncand, st, step_ms, clocks=None):
     multiplication: integer multiply-add, no memory traffic to speak of (the
     candidate list is read once).  The ceiling is the same arithmetic run
     register-resident at full occupancy on this GPU (fs_bench_int_pipe kinds
-    4-9: the walk's own PTX step blocks and the Montgomery product), so
+    4-13: the walk's own PTX step blocks and the Montgomery product), so
     peak = pair-steps the kernel would finish if its walk ran at the walk
     ceiling and its setup at the Montgomery-product ceiling."""
     pmin, pmax, nmin, nmax, seg = WORKLOADS[wl]
@@ -148,7 +148,7 @@ def roofline(ctx, fs, wl, ncand, st, step_ms, clocks=None):
                      "imad_lane_ops_per_s": imad_ops},
         "setup_products_per_candidate": smp,
         "peak_source": "measured on this GPU: the walk step's PTX block and mont_mul, register-resident at full "
-                       "occupancy (fs_bench_int_pipe kinds 4-9)",
+                       "occupancy (fs_bench_int_pipe kinds 4-13)",
         "imad_pipe_busy_ncu": cap.get("imad_pipe_busy"), "ncu_source": cap.get("source"),
         "hbm": {"achieved": hbm_ach, "peak": hbm_peak, "unit": "GB/s",
                 "frac": hbm_ach / hbm_peak if hbm_peak else None,
