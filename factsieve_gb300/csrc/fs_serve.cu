@@ -359,8 +359,25 @@ extern "C" int fs_serve_round(fs_ctx* c, uint32_t* n_active, uint32_t* n_queued)
         ch.layer_begin = 0;
         ch.layer_end = j.nlayers;
         ch.tag = (u32)j.slot;
-        if (j.state == fs_serve::SETUP) {
-            const double per = 2.7 * (double)j.nwords + 64.0;
+        const double per = 2.7 * (double)j.nwords + 64.0;   // setup cost per candidate, in walk-step units
+        const double whole = (double)j.ncand * (per + (double)(j.spec.nmax - j.spec.nmin));
+        if (j.state == fs_serve::SETUP && j.setup_next == 0 && whole <= std::max(budget, 0.0)) {
+            // the whole job fits the round: starting residues, the walk and the
+            // checksum in one chunk (one round instead of two or more)
+            ch.first = 0;
+            ch.count = j.ncand;
+            ch.flags = fs::SERVE_SETUP | fs::SERVE_FINAL;
+            ch.nstart = j.spec.nmin;
+            ch.nend = j.spec.nmax;
+            j.setup_next = j.ncand;
+            j.walk_n = j.spec.nmax;
+            j.state = fs_serve::WALK;
+            j.final_queued = true;
+            j.final_round = R;
+            budget -= whole;
+            s.setup_units += per * j.ncand;
+            s.served_steps += (uint64_t)j.ncand * (uint64_t)(j.spec.nmax - j.spec.nmin);
+        } else if (j.state == fs_serve::SETUP) {
             uint64_t cnt = (uint64_t)std::max(4096.0, std::max(budget, 0.0) / per);
             cnt = (cnt + fs::kTileCandidates - 1) / fs::kTileCandidates * fs::kTileCandidates;
             ch.first = j.setup_next;

@@ -9,13 +9,15 @@ pytestmark = pytest.mark.gpu
 from test_gpu_batch import JOBS
 
 
-def test_served_jobs_equal_each_job_alone(ctx):
+@pytest.mark.parametrize("budget", [100_000_000, 2_000_000_000, 10**13])
+def test_served_jobs_equal_each_job_alone(ctx, budget):
+    """A small round budget forces many rounds (setup split over candidates,
+    walks split into chunks, jobs joining while others are mid-walk); a large
+    one serves each job whole in one chunk; 2e9 mixes both."""
     import factsieve_gb300 as fs
     from factsieve_gb300.serve import Server
     alone = {k: ctx.sieve(*j, threads=8) for k, j in enumerate(JOBS)}
-    # a small round budget forces many rounds: setup split over candidates,
-    # walks split into chunks, jobs joining while others are mid-walk
-    srv = Server(ctx, max_active=3, round_budget=2_000_000_000, mem_reserve=1 << 30)
+    srv = Server(ctx, max_active=3, round_budget=budget, mem_reserve=1 << 30)
     done = {}
     pending = list(enumerate(JOBS))
     rounds = 0
@@ -31,7 +33,7 @@ def test_served_jobs_equal_each_job_alone(ctx):
             assert rounds < 5000
     finally:
         srv.close()
-    assert rounds > len(JOBS)
+    assert rounds > len(JOBS) or budget >= 10**13
     for k, d in done.items():
         a = alone[k]
         kept, cs_add, disc = fs.postprocess(d["hits"], threads=8)
