@@ -57,8 +57,8 @@ IMAD_PER_PRODUCT = 20   # reference m_mul on 32-bit limbs (8 mul_wide + 4 + 8)
 # one ncu --set full capture of one launch of the same workload
 # (profiles/sieve_kernel_config2.md, profiles/sieve_kernel_config3.md)
 NCU_CAPTURE = {
-    "config2": {"traffic": 29_087_744, "imad_pipe_busy": 0.873, "source": "profiles/sieve_kernel_config2.md"},
-    "config3": {"traffic": 18_730_240, "imad_pipe_busy": 0.827, "source": "profiles/sieve_kernel_config3.md"},
+    "config2": {"traffic": 29_148_672, "imad_pipe_busy": 0.888, "source": "profiles/sieve_kernel_config2.md"},
+    "config3": {"traffic": 18_725_632, "imad_pipe_busy": 0.862, "source": "profiles/sieve_kernel_config3.md"},
 }
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 
