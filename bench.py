@@ -247,6 +247,25 @@ def cpu_slice_run(pmin, nmin, nmax, width):
     return r, dt
 
 
+def cpu_model() -> str:
+    """The host CPU's model name (/proc/cpuinfo; on Arm the implementer and part)."""
+    try:
+        with open("/proc/cpuinfo") as fh:
+            info = fh.read()
+    except OSError:
+        return "unknown"
+    for key in ("model name", "Model", "CPU part"):
+        for line in info.splitlines():
+            if line.startswith(key):
+                val = line.split(":", 1)[1].strip()
+                if key == "CPU part":
+                    impl = next((ln.split(":", 1)[1].strip() for ln in info.splitlines()
+                                 if ln.startswith("CPU implementer")), "?")
+                    return f"implementer {impl} part {val}"
+                return val
+    return "unknown"
+
+
 def cpu_baseline(wl, budget_s=40.0):
     """The oracle on all host cores: config 1 in full, configs 2 and 3 on the
     fixed contiguous 1/100 slice at the start of the p-range (the work is
@@ -264,6 +283,7 @@ def cpu_baseline(wl, budget_s=40.0):
     r, dt = cpu_slice_run(pmin, nmin, nmax, width)
     pairs = r["primecount"] * (nmax - nmin)
     return {"value": pairs / dt, "unit": "pair-steps/s", "cores": os.cpu_count(), "kind": "port",
+            "cpu": cpu_model(),
             "sample": f"{label}: p in [{pmin}, {pmin + width}) ({r['primecount']} candidates, "
                       f"n in [{nmin}, {nmax})), oracle/oracle.c OpenMP, {dt:.1f} s"}
 
@@ -297,6 +317,7 @@ def run_reference(args):
                    "step": f"a {width}-wide slice of the p-range per step (bounded CPU sample)",
                    "l2": "n/a (CPU)"},
         "cpu_baseline": {"value": value, "unit": "pair-steps/s", "cores": os.cpu_count(), "kind": "port",
+                         "cpu": cpu_model(),
                          "sample": f"{args.steps} consecutive {width}-wide p-slices, oracle/oracle.c OpenMP "
                                    f"(the reference's OpenCL path has no runtime on this host)"},
         "e2e": {"value": value, "unit": "pair-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
