@@ -127,8 +127,10 @@ __global__ void __launch_bounds__(kSieveThreads) setup_partial_kernel(SieveArgs 
 __global__ void __launch_bounds__(256) table_check_kernel(TableCheckArgs a) {
     __shared__ u64 part[256];
     __shared__ bool last;
-    if (*a.ncand == 0) return;
-    const Prime c = make_prime(a.cand[0]);
+    // the segment's first candidate, as the reference checks; a segment without
+    // candidates checks against the prime 2^61 - 1 instead, so the check never
+    // passes silently
+    const Prime c = make_prime(*a.ncand ? a.cand[0] : 2305843009213693951ull);
     u64 acc = c.one;   // deficit grows by one per factor k
     const u32 stride = gridDim.x * blockDim.x;
     for (u64 k = 2 + blockIdx.x * blockDim.x + threadIdx.x; k <= a.n0; k += stride)

@@ -143,3 +143,16 @@ def test_pending_count_sizes_collect(ctx, orc):
     assert (len(hits), raw, pc, rc) == (want["nhits"], want["raw_sum"], want["primecount"], 0)
     assert fs.lib().fs_search_pending(ctx.handle, fs._p64(pend)) == 0
     assert int(pend[0]) == 0                                                # collect cleared them
+
+
+@pytest.mark.parametrize("nmin", [127, 5000])
+def test_table_check_without_candidates_uses_a_fixed_prime(ctx, nmin):
+    """A segment with no candidate still checks the power table, against 2^61 - 1."""
+    import math
+    import torch
+    cand = torch.zeros(1, dtype=torch.int64, device="cuda")
+    ctr = torch.zeros(4, dtype=torch.int64, device="cuda")          # ncand = 0
+    direct, table = ctx.table_check(cand.data_ptr(), ctr.data_ptr(), nmin)
+    q = (1 << 61) - 1
+    assert direct == table == math.factorial(nmin) * (1 << 64) % q
+    assert int(_counters(ctr)["flags"]) == 0
