@@ -77,6 +77,9 @@ def test_cli_help_and_bad_arguments(fslib, tmp_path):
     (["-n", "3000", "-N", "2000", "-p", "1e6", "-P", "2e6"], "nmin <= nmax is required"),
     (["-n", "1000", "-N", "2000", "-p", "3e6", "-P", "2e6"], "pmin <= pmax is required"),
     (["-n", "2000", "-N", "3000", "-p", "1000", "-P", "2e6"], "pmin must be >= nmin"),
+    # -d/--device is accepted and ignored, as in the reference (main.cpp: handled, not used)
+    (["-d", "3", "-n", "3000", "-N", "2000", "-p", "1e6", "-P", "2e6"], "nmin <= nmax is required"),
+    (["--device=1", "-n", "3000", "-N", "2000", "-p", "1e6", "-P", "2e6"], "nmin <= nmax is required"),
 ])
 def test_cli_range_checks(fslib, tmp_path, args, msg):
     if not os.path.exists(fslib.CLI_PATH):
