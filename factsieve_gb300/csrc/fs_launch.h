@@ -116,8 +116,8 @@ struct ServeArgs {
     u32 hitcap;
 };
 
-cudaError_t launch_serve_round(const ServeArgs& a, int grid, cudaStream_t s);
-cudaError_t serve_occupancy(int* blocks_per_sm);
+cudaError_t launch_serve_round(const ServeArgs& a, int grid, cudaStream_t s, int ppt);
+cudaError_t serve_occupancy(int* blocks_per_sm, int ppt);
 cudaError_t launch_gen(const GenArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_batch(const BatchArgs& a, int grid, cudaStream_t s);
 cudaError_t batch_occupancy(int* blocks_per_sm);

@@ -106,19 +106,22 @@ __global__ void __launch_bounds__(kSieveThreads, 2) batch_sieve_kernel(BatchArgs
 
 // ============================================================ serving ====
 
-// One round of the serving loop: a list of tiles, each up to kTileCandidates
-// candidates of one job in one phase (starting residue from the plan, a
-// chunk of the walk, the final checksum), four per thread, taken from a
-// global counter by persistent blocks.  Residues live in each job's device
-// buffer between rounds.
-__global__ void __launch_bounds__(kSieveThreads, 2) serve_round_kernel(ServeArgs a) {
+// One round of the serving loop: a list of tiles, each up to PPT x 256
+// candidates of one job in one phase (starting residues from the plan, a
+// chunk of the walk, the final checksum), PPT candidates per thread, taken
+// from a global counter by persistent blocks.  Residues live in each job's
+// device buffer between rounds.  PPT = 4 (four chains per thread) is the
+// throughput form; PPT = 2 puts a small round's candidates on twice as many
+// SMs (lower latency when the GPU would otherwise idle).
+template <int PPT>
+__global__ void __launch_bounds__(kSieveThreads, PPT == 4 ? 2 : 3) serve_round_kernel(ServeArgs a) {
     __shared__ HitStage st;
     __shared__ u32 s_tile;
     __shared__ u64 wsum[kSieveThreads / 32];
     __shared__ u32 wbad[kSieveThreads / 32];
     if (threadIdx.x == 0) st.n = 0;
     __syncthreads();
-    const u32 per_tile = kTileCandidates;
+    const u32 per_tile = PPT * kSieveThreads;
     const u32 ntiles = a.nchunks ? a.chunks[a.nchunks - 1].tile_end : 0;
     for (;;) {
         if (threadIdx.x == 0) s_tile = atomicAdd(a.tile_counter, 1u);
@@ -135,37 +138,60 @@ __global__ void __launch_bounds__(kSieveThreads, 2) serve_round_kernel(ServeArgs
         }
         const ServeChunk T = a.chunks[lo];
         const u32 tile0 = lo ? a.chunks[lo - 1].tile_end : 0;
-        const u32 i0 = T.first + (t - tile0) * per_tile + 4 * threadIdx.x;
+        const u32 i0 = T.first + (t - tile0) * per_tile + PPT * threadIdx.x;
         const u32 end = T.first + T.count;
         u64 sum = 0;
         u32 bad = 0;
         if (i0 < end) {
             const WalkOut o{&st, a.hits, a.hitcap, a.gctr, (int)T.tag};
-            Prime c[4];
-            const u32 nreal = load_quad(T.cand, i0, end, c);
-            u64 r[4];
-            if (T.flags & SERVE_SETUP) {
-                plan_product4(c, T.words, T.layers, T.layer_begin, T.layer_end, r);
+            if constexpr (PPT == 4) {
+                Prime c[4];
+                const u32 nreal = load_quad(T.cand, i0, end, c);
+                u64 r[4];
+                if (T.flags & SERVE_SETUP) {
+                    plan_product4(c, T.words, T.layers, T.layer_begin, T.layer_end, r);
 #pragma unroll
-                for (int h = 0; h < 4; ++h)
-                    r[h] = mont_mul(r[h], mont_pow(c[h].r2, T.deficit, c[h]), c[h].p, c[h].pinv);
+                    for (int h = 0; h < 4; ++h)
+                        r[h] = mont_mul(r[h], mont_pow(c[h].r2, T.deficit, c[h]), c[h].p, c[h].pinv);
+                } else {
+                    r[0] = T.residue[i0];
+#pragma unroll
+                    for (int h = 1; h < 4; ++h) r[h] = (u32)h < nreal ? T.residue[i0 + h] : r[0];
+                }
+                walk_quad_rt((int)T.walk, r, c, nreal, T.nstart, T.nend, o);
+                if (T.flags & SERVE_FINAL) {
+#pragma unroll
+                    for (int h = 0; h < 4; ++h)
+                        if ((u32)h < nreal) final_check(c[h], r[h], T.nend, sum, bad);
+                } else {
+#pragma unroll
+                    for (int h = 0; h < 4; ++h)
+                        if ((u32)h < nreal) T.residue[i0 + h] = r[h];
+                }
             } else {
-                r[0] = T.residue[i0];
-#pragma unroll
-                for (int h = 1; h < 4; ++h) r[h] = (u32)h < nreal ? T.residue[i0 + h] : r[0];
-            }
-            walk_quad_rt((int)T.walk, r, c, nreal, T.nstart, T.nend, o);
-            if (T.flags & SERVE_FINAL) {
-#pragma unroll
-                for (int h = 0; h < 4; ++h)
-                    if ((u32)h < nreal) final_check(c[h], r[h], T.nend, sum, bad);
-            } else {
-#pragma unroll
-                for (int h = 0; h < 4; ++h)
-                    if ((u32)h < nreal) T.residue[i0 + h] = r[h];
+                const bool real_b = i0 + 1 < end;
+                const Prime ca = make_prime(T.cand[i0]);
+                const Prime cb = real_b ? make_prime(T.cand[i0 + 1]) : ca;
+                u64 ra, rb;
+                if (T.flags & SERVE_SETUP) {
+                    plan_product2(ca, cb, T.words, T.layers, T.layer_begin, T.layer_end, ra, rb);
+                    ra = mont_mul(ra, mont_pow(ca.r2, T.deficit, ca), ca.p, ca.pinv);
+                    rb = mont_mul(rb, mont_pow(cb.r2, T.deficit, cb), cb.p, cb.pinv);
+                } else {
+                    ra = T.residue[i0];
+                    rb = real_b ? T.residue[i0 + 1] : ra;
+                }
+                walk_pair(ra, rb, ca, cb, real_b, T.nstart, T.nend, o);
+                if (T.flags & SERVE_FINAL) {
+                    final_check(ca, ra, T.nend, sum, bad);
+                    if (real_b) final_check(cb, rb, T.nend, sum, bad);
+                } else {
+                    T.residue[i0] = ra;
+                    if (real_b) T.residue[i0 + 1] = rb;
+                }
             }
         }
-    if (T.flags & SERVE_FINAL) {
+        if (T.flags & SERVE_FINAL) {
 #pragma unroll
             for (int d = 16; d; d >>= 1) {
                 sum += __shfl_xor_sync(0xffffffffu, sum, d);
@@ -218,13 +244,16 @@ cudaError_t batch_occupancy(int* blocks_per_sm) {
 
 int batch_max_jobs() { return kBatchMaxJobs; }
 
-cudaError_t launch_serve_round(const ServeArgs& a, int grid, cudaStream_t s) {
-    serve_round_kernel<<<grid, kSieveThreads, 0, s>>>(a);
+cudaError_t launch_serve_round(const ServeArgs& a, int grid, cudaStream_t s, int ppt) {
+    if (ppt == 2) serve_round_kernel<2><<<grid, kSieveThreads, 0, s>>>(a);
+    else serve_round_kernel<4><<<grid, kSieveThreads, 0, s>>>(a);
     return cudaGetLastError();
 }
 
-cudaError_t serve_occupancy(int* blocks_per_sm) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, serve_round_kernel, kSieveThreads, 0);
+cudaError_t serve_occupancy(int* blocks_per_sm, int ppt) {
+    if (ppt == 2)
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, serve_round_kernel<2>, kSieveThreads, 0);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, serve_round_kernel<4>, kSieveThreads, 0);
 }
 
 }  // namespace fs

@@ -82,7 +82,7 @@ struct Server {
     int64_t inflight_id = -1;
     int64_t round_id = 0;                        // id of the next round
     uint32_t next_job = 0;                       // round-robin start slot
-    int grid = 1;
+    int grid4 = 1, grid2 = 1;                    // persistent grids of the 4- and 2-per-thread forms
     uint64_t rounds = 0, served_steps = 0;
     double setup_units = 0;                      // setup work queued, in walk-step units
     // CUDA events around each round kernel, read when drained
@@ -226,8 +226,11 @@ extern "C" int fs_serve_create(fs_ctx* c, const fs_serve_config* cfg) {
         SK(c, cudaMallocHost((void**)&s->stage[b], kStageBytes));
     }
     int occ = 0;
-    if (fs::serve_occupancy(&occ) != cudaSuccess || occ < 1) occ = 1;
-    s->grid = c->sm_count * occ;
+    if (fs::serve_occupancy(&occ, 4) != cudaSuccess || occ < 1) occ = 1;
+    s->grid4 = c->sm_count * occ;
+    occ = 0;
+    if (fs::serve_occupancy(&occ, 2) != cudaSuccess || occ < 1) occ = 1;
+    s->grid2 = c->sm_count * occ;
     return FS_OK;
 }
 
@@ -416,9 +419,15 @@ extern "C" int fs_serve_round(fs_ctx* c, uint32_t* n_active, uint32_t* n_queued)
         hc[nch++] = ch;
         s.next_job = (slot + 1) % S;
     }
+    // four candidates per thread, unless the round's tiles would not fill the
+    // GPU: then two per thread, twice the blocks, a shorter round
+    uint32_t tiles4 = 0;
+    for (uint32_t k = 0; k < nch; ++k) tiles4 += (hc[k].count + fs::kTileCandidates - 1) / fs::kTileCandidates;
+    const int ppt = tiles4 < (uint32_t)s.grid4 ? 2 : 4;
+    const uint32_t per_tile = (uint32_t)ppt * fs::sieve_threads();
     uint32_t tiles = 0;
     for (uint32_t k = 0; k < nch; ++k) {
-        tiles += (hc[k].count + fs::kTileCandidates - 1) / fs::kTileCandidates;
+        tiles += (hc[k].count + per_tile - 1) / per_tile;
         hc[k].tile_end = tiles;
     }
     // 2. queue the round
@@ -435,7 +444,7 @@ extern "C" int fs_serve_round(fs_ctx* c, uint32_t* n_active, uint32_t* n_queued)
         a.hits = s.d_hits[b];
         a.hitcap = s.cfg.hitcap;
         SK(c, cudaEventRecord(s.kev[b][0], c->stream));
-        SK(c, fs::launch_serve_round(a, std::min<int>(s.grid, (int)tiles), c->stream));
+        SK(c, fs::launch_serve_round(a, std::min<int>(ppt == 2 ? s.grid2 : s.grid4, (int)tiles), c->stream, ppt));
         SK(c, cudaEventRecord(s.kev[b][1], c->stream));
         s.kev_used[b] = true;
         ++c->launches;

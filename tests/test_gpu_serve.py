@@ -54,3 +54,31 @@ def test_admission_waits_for_device_memory(ctx):
         assert srv.poll() == []
     finally:
         srv.close()
+
+
+def test_large_round_in_four_candidate_form(ctx):
+    """Rounds with more tiles than the GPU holds run four candidates per thread,
+    small ones two (the other tests): both give each job's bits alone."""
+    import factsieve_gb300 as fs
+    from factsieve_gb300.serve import Server
+    jobs = [(10**12, 10**12 + 10**7, 100_000, 100_300), (2 * 10**12, 2 * 10**12 + 10**7, 50_000, 50_200),
+            ((1 << 63) + 1, (1 << 63) + 10**7, 1000, 1200)]
+    alone = {k: ctx.sieve(*j, threads=8) for k, j in enumerate(jobs)}
+    srv = Server(ctx, max_active=4, round_budget=10**13, mem_reserve=1 << 30)
+    done = {}
+    try:
+        for k, j in enumerate(jobs):
+            srv.submit(j, k)
+        rounds = 0
+        while len(done) < len(jobs):
+            srv.round()
+            rounds += 1
+            for d in srv.poll():
+                done[d["id"]] = d
+            assert rounds < 100
+    finally:
+        srv.close()
+    for k, d in done.items():
+        a = alone[k]
+        assert d["flags"] == 0
+        assert (d["primecount"], d["raw_sum"], len(d["hits"])) == (a.primecount, a.raw_sum, a.nhits), jobs[k]
