@@ -331,20 +331,20 @@ def test_known_large_factors_are_found(ctx, orc, variant, p, n, c):
     assert [(int(q), int(nc)) for q, nc in zip(r.factors["p"], r.factors["nc"])] == want["factors"]
 
 
-def _random_cases(n, seed):
+def _random_cases(n, seed, plo=1 << 7, wmax=6000):
     import math
     import random
     rng = random.Random(seed)
     out = []
     for _ in range(n):
-        lo = int(math.exp(rng.uniform(math.log(1 << 7), math.log((1 << 64) - 2_000_000))))
+        lo = int(math.exp(rng.uniform(math.log(plo), math.log((1 << 64) - 2_000_000))))
         width = rng.randrange(20_000, 120_000)
         nmin = int(math.exp(rng.uniform(math.log(34), math.log(300_000))))
-        out.append((max(lo, nmin), max(lo, nmin) + width, nmin, nmin + rng.randrange(1, 6000)))
+        out.append((max(lo, nmin), max(lo, nmin) + width, nmin, nmin + rng.randrange(1, wmax)))
     return out
 
 
-@pytest.mark.parametrize("lo,hi,nmin,nmax", _random_cases(64, 20261204))
+@pytest.mark.parametrize("lo,hi,nmin,nmax", _random_cases(64, 20261204) + _random_cases(64, 7, 1 << 31, 20_000))
 def test_random_ranges_match_oracle(ctx, orc, lo, hi, nmin, nmax):
     """Seeded random p-ranges (log-uniform over [2^7, 2^64)) and n-ranges (nmin
     log-uniform over [34, 3e5)): the whole search (launch-wide step, four
