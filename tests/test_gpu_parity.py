@@ -303,7 +303,7 @@ def test_four_candidate_kernel_matches_oracle(ctx, orc, variant, lo, hi, nmin, n
                          for p, nc in zip(want["factors"]["p"], want["factors"]["nc"])]
 
 
-# Prime factors p >= 2^36 of n! + c for small n (found by factoring n! +- 1;
+# Prime factors p >= 2^31 of n! + c for small n (found by factoring n! +- 1;
 # each is re-checked below with an exact factorial): real hits for the
 # lazy walks, including the half-offset forms.
 KNOWN_FACTORS = [(87178291199, 14, -1), (256443711677, 17, -1), (1713311273363831, 19, 1),
@@ -311,7 +311,10 @@ KNOWN_FACTORS = [(87178291199, 14, -1), (256443711677, 17, -1), (171331127336383
                  (4826713612027, 21, -1), (93799610095769647, 22, 1), (170006681813, 22, -1),
                  (148139754736864591, 23, 1), (498390560021687969, 23, -1), (625793187653, 24, -1),
                  (991459181683, 24, -1), (1042190196053, 28, -1), (2778942057555023489, 29, 1),
-                 (594278556271609021, 29, -1)]
+                 (594278556271609021, 29, -1),
+                 # 2^31 <= p < 2^36 (shifted-window step) and p >= 2^63 (96-bit half-offset step)
+                 (3790360487, 14, 1), (6880233439, 16, -1), (7798078091, 28, -1),
+                 (10398560889846739639, 34, -1)]
 
 
 @pytest.mark.parametrize("variant", [3, 5])
