@@ -4,8 +4,11 @@
                     [--workload config2|config3|config1]
 
 Workload (default config2, the plain large sieve): p in [1e12, 1e12 + 1e9),
-n in [1e5, 2e5).  One step = one p-segment of 1e8 (so 10 steps cover the
-configuration once), run through getsegprimes -> setup -> iterate -> check.
+n in [1e5, 2e5).  One step = one pass over the whole p-range as one segment
+(the command line's default segment width; wider segments leave a shorter
+partial last wave), run through getsegprimes -> setup -> iterate -> check.
+Config 3 steps are 1e8-wide segments (its measured best); --segment
+overrides the width (the ncu full capture uses 1e8).
 Metric: (p,n) pair-steps/s = candidates x (nmax - nmin) / time, plus the
 fraction of the integer-multiply roofline.
 
@@ -49,7 +52,7 @@ sys.path.insert(0, ROOT)
 WORKLOADS = {
     # name: (pmin, pmax, nmin, nmax, segment width)
     "config1": (1_000_000, 2_000_000, 1000, 2000, 1_000_000),      # a step is the whole (small) range
-    "config2": (1_000_000_000_000, 1_001_000_000_000, 100_000, 200_000, 100_000_000),
+    "config2": (1_000_000_000_000, 1_001_000_000_000, 100_000, 200_000, 1_000_000_000),   # a step: the whole range
     "config3": (1 << 63, (1 << 63) + 1_000_000_000, 1_000_000, 1_010_000, 100_000_000),
 }
 IMAD_PER_PRODUCT = 20   # reference m_mul on 32-bit limbs (8 mul_wide + 4 + 8)
@@ -57,7 +60,8 @@ IMAD_PER_PRODUCT = 20   # reference m_mul on 32-bit limbs (8 mul_wide + 4 + 8)
 # one ncu --set full capture of one launch of the same workload
 # (profiles/sieve_kernel_config2.md, profiles/sieve_kernel_config3.md)
 NCU_CAPTURE = {
-    "config2": {"traffic": 29_148_672, "imad_pipe_busy": 0.888, "source": "profiles/sieve_kernel_config2.md"},
+    # config 2: a 1e8-wide capture (29,182,720 B) scaled by 10 to the whole-range launch the bench times
+    "config2": {"traffic": 291_827_200, "imad_pipe_busy": 0.887, "source": "profiles/sieve_kernel_config2.md"},
     "config3": {"traffic": 18_725_632, "imad_pipe_busy": 0.862, "source": "profiles/sieve_kernel_config3.md"},
 }
 GOLDEN = os.path.join(ROOT, "tests", "golden")
@@ -98,7 +102,7 @@ def setup_products(fs, nmin: int) -> int:
     return len(words) + max(len(layers) - 1, 0) + pow_d + 1 + 10 + 2 + 3
 
 
-def roofline(ctx, fs, wl, ncand, st, step_ms, clocks=None):
+def roofline(ctx, fs, wl, ncand, st, step_ms, clocks=None, seg=None):
     """Roofline of the fused sieve kernel.  The work is 64-bit modular
     multiplication: integer multiply-add, no memory traffic to speak of (the
     candidate list is read once).  The ceiling is the same arithmetic run
@@ -106,9 +110,10 @@ def roofline(ctx, fs, wl, ncand, st, step_ms, clocks=None):
     4-13: the walk's own PTX step blocks and the Montgomery product), so
     peak = pair-steps the kernel would finish if its walk ran at the walk
     ceiling and its setup at the Montgomery-product ceiling."""
-    pmin, pmax, nmin, nmax, seg = WORKLOADS[wl]
+    pmin, pmax, nmin, nmax, seg0 = WORKLOADS[wl]
+    seg = seg or seg0
     W = nmax - nmin
-    step = fs.walk_step(pmin, pmin + seg, nmax)
+    step = fs.walk_step(pmin, min(pmin + seg, pmax), nmax)
     kind, step_name = STEP_CEILING_KIND[step]
     walk_ceil, _ = ctx.bench_int_pipe(kind, 4000)
     mm_ceil, _ = ctx.bench_int_pipe(4, 4000)
@@ -338,6 +343,8 @@ def run_ours(args):
     dist = init_dist(ws, "nccl" if ws > 1 else None)
     wl = args.workload
     pmin, pmax, nmin, nmax, seg = WORKLOADS[wl]
+    if args.segment:
+        seg = int(args.segment)
     W = nmax - nmin
     nseg = (pmax - pmin + seg - 1) // seg
 
@@ -394,7 +401,7 @@ def run_ours(args):
 
     # roofline of the dominant kernel, from this rank's events
     my_pc = primecount if not dist else int(t[4].item())
-    roof = roofline(ctx, fs, wl, my_pc, st, ms, clk.summary())
+    roof = roofline(ctx, fs, wl, my_pc, st, ms, clk.summary(), seg)
 
     # e2e through the public API with host buffers, on rank 0's first segments
     e2e = None
@@ -600,6 +607,8 @@ def main():
     ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS) + ["config4", "config5"])
     ap.add_argument("--serve-seconds", type=float, default=180.0, help="config5: stop the replay after this long")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--segment", type=float, default=0,
+                    help="p-width of one step (default: the workload's; e.g. 1e8 for a short profiling case)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
