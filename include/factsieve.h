@@ -3,10 +3,10 @@
  *
  * The library replaces the reference's device layer: the OpenCL shim
  * (simpleCL.h:67-117) plus the kernels getsegprimes, setup, iterate, check,
- * clearn, clearresult and verify* (kernels/*.cl), and carries the host
- * pieces of the same path (power table, CPU factor verification).  Every
- * function returns a status code (FS_OK or FS_E_*) and never exits the
- * process; the reference printed and called exit() on any error
+ * clearn, clearresult and the verify kernels of the kernels directory, and
+ * carries the host pieces of the same path (power table, CPU factor
+ * verification).  Every function returns a status code (FS_OK or FS_E_*)
+ * and never exits the process; the reference printed and called exit() on any error
  * (simpleCL.c:347, cl_sieve.cpp:451-476).
  *
  * Threading: one fs_ctx per host thread; calls on one context are not

@@ -155,3 +155,28 @@ def test_walk_step_selection_boundaries(fslib):
     assert ws(10**13, 10**13 + 30_000, 1 << 28) == ANY                      # k_max >= 2^28: generic
     assert ws((1 << 63) - 1000, (1 << 63) + 1000, 5000) == ANY              # straddles 2^63
     assert ws(5, 5, 100) == ANY and ws(10**12, 10**12 + 5, 0) == ANY        # empty ranges
+
+
+def test_c_caller(fslib, tmp_path):
+    """The header and library serve a plain C program (gcc, no C++ or Python in between)."""
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    exe = str(tmp_path / "c_abi_example")
+    libdir = os.path.dirname(fslib.LIB_PATH)
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "c_abi_example.c"), "-L", libdir, "-lfactsieve",
+                    "-Wl,-rpath," + libdir, "-o", exe], check=True, capture_output=True, text=True)
+    out = subprocess.run([exe], check=True, capture_output=True, text=True, timeout=60).stdout
+    got = dict(line.split(" ", 1) for line in out.strip().splitlines())
+    assert got["parse_p"] == "0 1000000000000" and got["parse_P"] == "0 1001000000000"
+    assert got["parse_n"] == "0 100000" and got["bad_arg"] != "0"
+    assert got["is_prime"] == "1 0"
+    assert got["verify"] == "1 0 1"
+    rc, kept, cs, disc, first = got["postprocess"].split()
+    assert (rc, kept, disc, first) == ("0", "2", "0", "149")          # sorted by (p, |n|), both kept
+    assert int(cs) == (25 - 1) + (169725 + 1)                          # checksum += n + c per kept factor
+    assert int(got["capacity"]) == fslib.candidate_capacity(10**12, 10**12 + 10**8)
+    assert got["walk_step"] == "4 6"
+    assert got["strerror"].strip() == fslib.lib().fs_strerror(fslib.FS_E_OVERFLOW).decode()
