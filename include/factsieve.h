@@ -6,8 +6,8 @@
  * clearn, clearresult and the verify kernels of the kernels directory, and
  * carries the host pieces of the same path (power table, CPU factor
  * verification).  Every function returns a status code (FS_OK or FS_E_*)
- * and never exits the process; the reference printed and called exit() on any error
- * (simpleCL.c:347, cl_sieve.cpp:451-476).
+ * and never exits the process; the reference printed and called exit() on
+ * any error (simpleCL.c:347, cl_sieve.cpp:451-476).
  *
  * Threading: one fs_ctx per host thread; calls on one context are not
  * thread-safe.  Device buffers of a search belong to the context; host
