@@ -165,9 +165,12 @@ int setup_search(WorkStatus& st, SearchOptions& so) {
 // p-width of a segment: about 2e11 (p,n) steps of GPU work, or the whole range.
 uint64_t segment_width(const WorkStatus& st, const SearchOptions& so) {
     if (so.seg_width) return so.seg_width;
+    // about 1.5e12 (p,n) steps per segment (under a second on a GB300): long
+    // enough that the last partial wave of a launch costs little, short
+    // enough for a progress line every second or so
     const double lp = std::log(std::max<double>((double)st.p, 3.0));
     const double per_cand = (double)(st.nmax - st.nmin) + 0.036 * st.nmin + 64.0;
-    double w = 2e11 * lp / per_cand;
+    double w = 1.5e12 * lp / per_cand;
     w = std::min(std::max(w, 1e5), 4e9);
     return (uint64_t)w;
 }
