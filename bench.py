@@ -84,6 +84,7 @@ def reference_setup_products(nmin: int) -> int:
 
 # Ceiling microkernels (fs_bench_int_pipe kinds) of each residue step.
 STEP_CEILING_KIND = {6: (11, "32-bit half-offset step"), 7: (12, "shifted-window half-offset 64-bit step"),
+                     9: (14, "half-offset 64-bit step, quotient on the FP32 pipe"),
                      4: (5, "half-offset lazy 64-bit step"),
                      5: (10, "half-offset lazy 96-bit step"), 8: (13, "half-offset canonical 96-bit step"),
                      1: (6, "lazy 64-bit step"),
@@ -153,7 +154,7 @@ def roofline(ctx, fs, wl, ncand, st, step_ms, clocks=None, seg=None):
                      "imad_lane_ops_per_s": imad_ops},
         "setup_products_per_candidate": smp,
         "peak_source": "measured on this GPU: the walk step's PTX block and mont_mul, register-resident at full "
-                       "occupancy (fs_bench_int_pipe kinds 4-13)",
+                       "occupancy (fs_bench_int_pipe kinds 4-14)",
         "imad_pipe_busy_ncu": cap.get("imad_pipe_busy"), "ncu_source": cap.get("source"),
         "hbm": {"achieved": hbm_ach, "peak": hbm_peak, "unit": "GB/s",
                 "frac": hbm_ach / hbm_peak if hbm_peak else None,

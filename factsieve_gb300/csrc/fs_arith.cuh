@@ -249,6 +249,7 @@ __device__ __forceinline__ u32 recip_pow2(u64 p, int e) {
 
 __device__ __forceinline__ int bitlen64(u64 x) { return 64 - __clzll(x); }
 __device__ __forceinline__ int bitlen32(u32 x) { return 32 - __clz(x); }
+__device__ __forceinline__ u64 umin64(u64 a, u64 b) { return a < b ? a : b; }
 
 struct Lazy96 {
     u64 p, one;
@@ -494,6 +495,131 @@ __device__ __forceinline__ u32 half_walk8x2(u32& al, u32& ah, u32& bl, u32& bh, 
         : "+r"(al), "+r"(ah), "+r"(bl), "+r"(bh), "=r"(flag)
         : "r"(k1), "r"(A.np0), "r"(A.np1), "r"(A.M), "r"(A.x0), "r"(A.x1), "r"(B.np0), "r"(B.np1), "r"(B.M),
           "r"(B.x0), "r"(B.x1));
+    return flag;
+}
+
+// ------------- iterate: half-offset 64-bit steps, quotient on the FP32 pipe --
+//
+// The half-offset lazy 64-bit step runs five products on the integer multiply
+// pipe, which bounds the walk.  This step takes the quotient estimate on the
+// FP32 pipe instead and keeps four.  Let s = bitlen(f) - 4 for a floor
+// f <= p with s >= 35, z = floor(t / 2^s) and Mf = 2^s/p rounded down to
+// 24 bits.  The estimate floor(z Mf) comes from three exact float
+// instructions:
+//   1. A funnel shift of t's high word, with 2^(s-35) shifted in above it,
+//      gives the bit pattern of the float F = 2^-63 + z 2^-86.  Its exponent
+//      field is 64 and its mantissa is z, which needs z < 2^23.
+//   2. F - 2^-63 = z 2^-86 is exact by Sterbenz's lemma.
+//   3. fma rounding down, by Mf 2^-63, gives z Mf 2^-149.  That lies below
+//      2^-126, on the subnormal grid, so its bit pattern is the integer
+//      floor(z Mf).
+// The estimate never exceeds t/p.  It falls short of it by less than
+// 1 + 2^s/p + (t/p) 2^-23, which is below 1 + 1/8 + 1/16 when
+// r < (19/16) p and 19 k_max <= 2^23.  So r stays below (19/16) p < x + p,
+// and the exact test is r in {x, x + 1}, as in the half-offset lazy step.
+// Validity over a launch, with f the thread's least candidate: p >= 2^38,
+// p k_max <= 2^62, 19 k_max <= 2^23, and 19 p_max k_max <
+// 2^(bitlen(p_min) + 23), which keeps z < 2^23.  The two float instructions
+// have no .ftz, so subnormals are kept.
+struct HalfF {
+    u64 p, x;
+    u32 np0, np1;             // 2^64 - p
+    float mf;                 // (2^s/p rounded down to 24 bits) 2^-63
+    u32 sh, hc;               // s - 32 and 2^(s - 35): the funnel shift that builds F
+    u32 x0, x1;               // low words of x and x + 1
+};
+
+__device__ __forceinline__ bool halff_ok(u64 p, u32 kmax) {
+    if (p < (1ull << 38) || kmax == 0 || 19ull * kmax > (1ull << 23) || p > (1ull << 62) / kmax) return false;
+    const u64 v = p * (u64)kmax;                       // exact: p kmax <= 2^62
+    const u64 hi = __umul64hi(v, 19ull), lo = v * 19ull;
+    const int e = bitlen64(p) + 23;                    // 19 p k_max < 2^e
+    return e >= 64 ? (hi >> (e - 64)) == 0 : (hi == 0 && (lo >> e) == 0);
+}
+
+// f <= p: the floor that sets s (the least candidate of the thread, whose
+// launch-wide validity the host has shown, or p itself).
+__device__ __forceinline__ HalfF make_halff(const Prime& c, u64 f) {
+    HalfF H;
+    H.p = c.p;
+    H.x = (c.p - 1) >> 1;
+    const u64 np = 0ull - c.p;
+    H.np0 = (u32)np;
+    H.np1 = (u32)(np >> 32);
+    const int bl = bitlen64(c.p), s = bitlen64(f) - 4, e = bl + 23;
+    // m = floor(2^e / p) in [2^23, 2^24): 2^s/p rounded down to 24 bits is m 2^(s-e)
+    const u32 m = e <= 64 ? (u32)(((~0ull) / c.p) >> (64 - e)) : recip_pow2(c.p, e);
+    // m 2^(s - e - 63) as a float: exponent field s - bl + 64 (normal), mantissa m - 2^23
+    H.mf = __uint_as_float(((u32)(s - bl + 63) << 23) + m);
+    H.sh = (u32)(s - 32);
+    H.hc = 1u << (s - 35);
+    H.x0 = (u32)H.x;
+    H.x1 = (u32)(H.x + 1);
+    return H;
+}
+
+// floor(z Mf) from t's high word, as the PTX block computes it.
+__device__ __forceinline__ u32 halff_quot(u32 th, const HalfF& H) {
+    u32 q;
+    asm("{\n\t"
+        ".reg .b32 z;\n\t"
+        ".reg .f32 f;\n\t"
+        "shf.r.wrap.b32 z, %1, %2, %3;\n\t"
+        "mov.b32 f, z;\n\t"
+        "sub.rn.f32 f, f, 0f20000000;\n\t"
+        "fma.rm.f32 f, f, %4, 0f00000000;\n\t"
+        "mov.b32 %0, f;\n\t"
+        "}"
+        : "=r"(q)
+        : "r"(th), "r"(H.hc), "r"(H.sh), "f"(H.mf));
+    return q;
+}
+
+__device__ __forceinline__ u64 halff_step(u64 r, u32 k, const HalfF& H) {
+    const u64 t = r * (u64)k;
+    const u32 q = halff_quot((u32)(t >> 32), H);
+    return t + (u64)q * (((u64)H.np1 << 32) | H.np0);
+}
+__device__ __forceinline__ u64 halff_canon(u64 r, const HalfF& H) { return r >= H.p ? r - H.p : r; }
+
+#define FS_HFF_MUL(RL, RH, NP0, NP1, MF, SH, HC, T, R, TL, TH, Q, Z, F) \
+    "mul.wide.u32 " T ", " RL ", kk;\n\t"                                \
+    "mov.b64 {" TL ", " TH "}, " T ";\n\t"                               \
+    "mad.lo.u32 " TH ", " RH ", kk, " TH ";\n\t"                         \
+    "shf.r.wrap.b32 " Z ", " TH ", " HC ", " SH ";\n\t"                  \
+    "mov.b32 " F ", " Z ";\n\t"                                          \
+    "sub.rn.f32 " F ", " F ", 0f20000000;\n\t"                           \
+    "fma.rm.f32 " F ", " F ", " MF ", 0f00000000;\n\t"                   \
+    "mov.b32 " Q ", " F ";\n\t"                                          \
+    "mov.b64 " T ", {" TL ", " TH "};\n\t"                               \
+    "mad.wide.u32 " R ", " Q ", " NP0 ", " T ";\n\t"                     \
+    "mov.b64 {" RL ", " RH "}, " R ";\n\t"                               \
+    "mad.lo.u32 " RH ", " Q ", " NP1 ", " RH ";\n\t"
+#define FS_HFF_STEP2(J)                                                                              \
+    "add.u32 kk, %5, " #J ";\n\t"                                                                    \
+    FS_HF_TEST("%0", "%9", "%10")                                                                    \
+    FS_HF_TEST("%2", "%16", "%17")                                                                   \
+    FS_HFF_MUL("%0", "%1", "%6", "%7", "%8", "%11", "%12", "TA", "RA", "aL", "aH", "qA", "zA", "fA") \
+    FS_HFF_MUL("%2", "%3", "%13", "%14", "%15", "%18", "%19", "TB", "RB", "bL", "bH", "qB", "zB", "fB")
+
+// Eight float-quotient half-offset steps on two residues; the flag as
+// lazy_walk8x2's.
+__device__ __forceinline__ u32 halff_walk8x2(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const HalfF& A,
+                                             const HalfF& B) {
+    u32 flag;
+    asm("{\n\t"
+        ".reg .u32 kk, aL, aH, qA, zA, bL, bH, qB, zB;\n\t"
+        ".reg .f32 fA, fB;\n\t"
+        ".reg .u64 TA, RA, TB, RB;\n\t"
+        ".reg .pred P;\n\t"
+        "setp.ne.u32 P, %5, %5;\n\t"
+        FS_HFF_STEP2(0) FS_HFF_STEP2(1) FS_HFF_STEP2(2) FS_HFF_STEP2(3)
+        FS_HFF_STEP2(4) FS_HFF_STEP2(5) FS_HFF_STEP2(6) FS_HFF_STEP2(7)
+        "selp.u32 %4, 1, 0, P;\n\t"
+        "}"
+        : "+r"(al), "+r"(ah), "+r"(bl), "+r"(bh), "=r"(flag)
+        : "r"(k1), "r"(A.np0), "r"(A.np1), "f"(A.mf), "r"(A.x0), "r"(A.x1), "r"(A.sh), "r"(A.hc),
+          "r"(B.np0), "r"(B.np1), "f"(B.mf), "r"(B.x0), "r"(B.x1), "r"(B.sh), "r"(B.hc));
     return flag;
 }
 

@@ -748,7 +748,7 @@ int fs_plan_check(fs_ctx* c, const uint64_t* d_cand, fs_counters* d_ctr, uint32_
 int fs_walk_step(uint64_t plo, uint64_t phi, uint32_t kmax) { return fs::walk_for_range(plo, phi, kmax); }
 
 int fs_bench_int_pipe(fs_ctx* c, uint32_t kind, uint32_t iters, double* ops_per_sec, double* ms) {
-    if (!c || kind > 13 || iters == 0 || iters > (1u << 24)) return FS_E_ARG;
+    if (!c || kind > 14 || iters == 0 || iters > (1u << 24)) return FS_E_ARG;
     int rc = bind(c);
     if (rc) return rc;
     const int grid = c->sm_count * 8;   // 8 x 256 threads = 2048 per SM

@@ -246,7 +246,8 @@ __global__ void __launch_bounds__(256) imad_bench_kernel(u32 iters, u32 kind, u3
 //   kind 11 32-bit half-offset steps (half32_walk8x2), 4 chains
 //   kind 12 shifted-window half-offset 64-bit steps (halfmid_walk8x2), 4 chains
 //   kind 13 half-offset canonical 96-bit steps (canon96h_walk8x2), 4 chains
-constexpr u32 kCeilUnits[14] = {0, 0, 0, 0, 8, 32, 32, 32, 32, 4, 32, 32, 32, 32};
+//   kind 14 half-offset 64-bit steps, quotient on the FP32 pipe (halff_walk8x2), 4 chains
+constexpr u32 kCeilUnits[15] = {0, 0, 0, 0, 8, 32, 32, 32, 32, 4, 32, 32, 32, 32, 32};
 
 template <u32 kind>
 __global__ void __launch_bounds__(256) ceiling_kernel(u32 iters, u32 seed, u32* sink) {
@@ -255,6 +256,7 @@ __global__ void __launch_bounds__(256) ceiling_kernel(u32 iters, u32 seed, u32* 
     u64 base;
     switch (kind) {
         case 5: base = 1000000000000ull; break;           // 2^36 <= p, p kmax <= 2^62
+        case 14: base = 1000000000000ull; break;          // 2^38 <= p, 19 p kmax < 2^(bitlen(p) + 23)
         case 6: base = (1ull << 34) + 1; break;           // 2^33 < p < 2^36
         case 7: base = 1000000000000000ull; break;        // p kmax > 2^62, p < 2^63
         case 10: base = 1000000000000000ull; break;       // p kmax > 2^60, p < 2^63
@@ -309,6 +311,14 @@ __global__ void __launch_bounds__(256) ceiling_kernel(u32 iters, u32 seed, u32* 
             for (u32 it = 0; it < iters; ++it) {
                 acc += half_walk8x2(l[0], hh[0], l[1], hh[1], k0 + 8 * it, A, B);
                 acc += half_walk8x2(l[2], hh[2], l[3], hh[3], k0 + 8 * it, C, D);
+            }
+        } else if constexpr (kind == 14) {
+            const u64 f = umin64(umin64(c[0].p, c[1].p), umin64(c[2].p, c[3].p));
+            const HalfF A = make_halff(c[0], f), B = make_halff(c[1], f);
+            const HalfF C = make_halff(c[2], f), D = make_halff(c[3], f);
+            for (u32 it = 0; it < iters; ++it) {
+                acc += halff_walk8x2(l[0], hh[0], l[1], hh[1], k0 + 8 * it, A, B);
+                acc += halff_walk8x2(l[2], hh[2], l[3], hh[3], k0 + 8 * it, C, D);
             }
         } else if constexpr (kind == 6) {
             const Lazy64 A = make_lazy(c[0]), B = make_lazy(c[1]), C = make_lazy(c[2]), D = make_lazy(c[3]);
@@ -403,12 +413,13 @@ cudaError_t launch_imad_bench(u32 iters, u32 kind, u32 seed, u32* sink, int grid
         case 11: ceiling_kernel<11><<<grid, 256, 0, s>>>(iters, seed, sink); break;
         case 12: ceiling_kernel<12><<<grid, 256, 0, s>>>(iters, seed, sink); break;
         case 13: ceiling_kernel<13><<<grid, 256, 0, s>>>(iters, seed, sink); break;
+        case 14: ceiling_kernel<14><<<grid, 256, 0, s>>>(iters, seed, sink); break;
         default: imad_bench_kernel<<<grid, 256, 0, s>>>(iters, kind, seed, sink); break;
     }
     return cudaGetLastError();
 }
 
-double bench_units_per_thread_iter(u32 kind) { return kind < 4 ? 8.0 : (kind < 14 ? kCeilUnits[kind] : 0.0); }
+double bench_units_per_thread_iter(u32 kind) { return kind < 4 ? 8.0 : (kind < 15 ? kCeilUnits[kind] : 0.0); }
 
 int walk_for_range(uint64_t plo, uint64_t phi, uint32_t kmax) {
     if (phi <= plo || kmax == 0) return WALK_ANY;
@@ -418,6 +429,12 @@ int walk_for_range(uint64_t plo, uint64_t phi, uint32_t kmax) {
     if (plo > 2 && pmax < (1ull << 31) && kb <= 26) return WALK_H32;
     // the shifted-window half-offset step needs 2^31 <= p < 2^36 and kmax < 2^25 (halfmid_ok)
     if (plo >= (1ull << 31) && pmax < (1ull << 36) && kb <= 25) return WALK_HM;
+    // the float-quotient half-offset step needs p >= 2^38, p kmax <= 2^62,
+    // 19 kmax <= 2^23 and 19 pmax kmax < 2^(bitlen(plo) + 23) (halff_ok, with
+    // s taken from a thread's least candidate)
+    if (plo >= (1ull << 38) && pmax <= ((1ull << 62) / kmax) && 19ull * kmax <= (1ull << 23) &&
+        (unsigned __int128)19 * pmax * kmax < ((unsigned __int128)1 << ((64 - __builtin_clzll(plo)) + 23)))
+        return WALK_HF;
     // the half-offset lazy step needs p >= 2^36 and p kmax <= 2^62 (half_ok)
     if (plo >= (1ull << 36) && pmax <= ((1ull << 62) / kmax)) return WALK_H64;
     // the lazy 64-bit step needs p > 2^33 and p kmax <= 2^62 (lazy_ok)

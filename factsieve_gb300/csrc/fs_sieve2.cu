@@ -21,6 +21,7 @@ static void launch_sieve_w(const SieveArgs& a, int setup, bool fin, int grid, cu
 
 cudaError_t launch_sieve_pair(const SieveArgs& a, int setup, bool final_chunk, int grid, cudaStream_t s, int walk) {
     switch (walk) {
+        case WALK_HF: launch_sieve_w<3, WALK_HF>(a, setup, final_chunk, grid, s); break;
         case WALK_H64: launch_sieve_w<3, WALK_H64>(a, setup, final_chunk, grid, s); break;
         case WALK_H96: launch_sieve_w<3, WALK_H96>(a, setup, final_chunk, grid, s); break;
         case WALK_H32: launch_sieve_w<3, WALK_H32>(a, setup, final_chunk, grid, s); break;

@@ -180,7 +180,7 @@ struct WalkOut {
 // (p | n! + 1), 0 for neither.
 struct RegT64 {
     using K = Lazy64;
-    static __device__ __forceinline__ K make(const Prime& c, u32) { return make_lazy(c); }
+    static __device__ __forceinline__ K make(const Prime& c, u32, u64) { return make_lazy(c); }
     static __device__ __forceinline__ u32 block(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const K& A, const K& B) {
         return lazy_walk8x2(al, ah, bl, bh, k1, A, B);
     }
@@ -194,7 +194,7 @@ struct RegT64 {
 };
 struct RegL96 {
     using K = Lazy96;
-    static __device__ __forceinline__ K make(const Prime& c, u32 kmax) { return make_lazy96(c, kmax); }
+    static __device__ __forceinline__ K make(const Prime& c, u32 kmax, u64) { return make_lazy96(c, kmax); }
     static __device__ __forceinline__ u32 block(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const K& A, const K& B) {
         return lazy96_walk8x2(al, ah, bl, bh, k1, A, B);
     }
@@ -208,7 +208,7 @@ struct RegL96 {
 };
 struct RegC96 {
     using K = Canon96;
-    static __device__ __forceinline__ K make(const Prime& c, u32 kmax) { return make_canon96(c, kmax); }
+    static __device__ __forceinline__ K make(const Prime& c, u32 kmax, u64) { return make_canon96(c, kmax); }
     static __device__ __forceinline__ u32 block(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const K& A, const K& B) {
         return canon96_walk8x2(al, ah, bl, bh, k1, A, B);
     }
@@ -222,7 +222,7 @@ struct RegC96 {
 };
 struct RegH64 {
     using K = Half64;
-    static __device__ __forceinline__ K make(const Prime& c, u32) { return make_half(c); }
+    static __device__ __forceinline__ K make(const Prime& c, u32, u64) { return make_half(c); }
     static __device__ __forceinline__ u32 block(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const K& A, const K& B) {
         return half_walk8x2(al, ah, bl, bh, k1, A, B);
     }
@@ -234,9 +234,23 @@ struct RegH64 {
     }
     static __device__ __forceinline__ int hit(u64 c, const K& X) { return c == X.x ? -1 : (c == X.x + 1 ? 1 : 0); }
 };
+struct RegHF {
+    using K = HalfF;
+    static __device__ __forceinline__ K make(const Prime& c, u32, u64 f) { return make_halff(c, f); }
+    static __device__ __forceinline__ u32 block(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const K& A, const K& B) {
+        return halff_walk8x2(al, ah, bl, bh, k1, A, B);
+    }
+    static __device__ __forceinline__ u64 step(u64 r, u32 k, const K& X) { return halff_step(r, k, X); }
+    static __device__ __forceinline__ u64 canon(u64 r, const K& X) { return halff_canon(r, X); }
+    static __device__ __forceinline__ u64 enter(u64 r, const Prime& c, const K& X) { return half_enter(r, c, X.x); }
+    static __device__ __forceinline__ u64 leave(u64 r, const Prime& c, const K& X) {
+        return half_leave(halff_canon(r, X), c);
+    }
+    static __device__ __forceinline__ int hit(u64 c, const K& X) { return c == X.x ? -1 : (c == X.x + 1 ? 1 : 0); }
+};
 struct RegH32 {
     using K = Half32;
-    static __device__ __forceinline__ K make(const Prime& c, u32 kmax) { return make_half32(c, kmax); }
+    static __device__ __forceinline__ K make(const Prime& c, u32 kmax, u64) { return make_half32(c, kmax); }
     static __device__ __forceinline__ u32 block(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const K& A, const K& B) {
         return half32_walk8x2(al, ah, bl, bh, k1, A, B);
     }
@@ -250,7 +264,7 @@ struct RegH32 {
 };
 struct RegHM {
     using K = Half96;
-    static __device__ __forceinline__ K make(const Prime& c, u32 kmax) { return make_halfmid(c, kmax); }
+    static __device__ __forceinline__ K make(const Prime& c, u32 kmax, u64) { return make_halfmid(c, kmax); }
     static __device__ __forceinline__ u32 block(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const K& A, const K& B) {
         return halfmid_walk8x2(al, ah, bl, bh, k1, A, B);
     }
@@ -264,7 +278,7 @@ struct RegHM {
 };
 struct RegC96H {
     using K = Canon96H;
-    static __device__ __forceinline__ K make(const Prime& c, u32 kmax) { return make_canon96h(c, kmax); }
+    static __device__ __forceinline__ K make(const Prime& c, u32 kmax, u64) { return make_canon96h(c, kmax); }
     static __device__ __forceinline__ u32 block(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const K& A, const K& B) {
         return canon96h_walk8x2(al, ah, bl, bh, k1, A, B);
     }
@@ -276,7 +290,7 @@ struct RegC96H {
 };
 struct RegH96 {
     using K = Half96;
-    static __device__ __forceinline__ K make(const Prime& c, u32 kmax) { return make_half96(c, kmax); }
+    static __device__ __forceinline__ K make(const Prime& c, u32 kmax, u64) { return make_half96(c, kmax); }
     static __device__ __forceinline__ u32 block(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const K& A, const K& B) {
         return half96_walk8x2(al, ah, bl, bh, k1, A, B);
     }
@@ -296,14 +310,18 @@ __device__ __forceinline__ void reg_check(u64 r, u32 n, const typename Reg::K& X
     if (h) record_hit(*o.st, X.p, h * (int)n, o.hits, o.hitcap, o.ctr, o.tag);
 }
 
-// Replay eight steps from r at n0 with exact tests (the PTX block saw a
-// possible hit in them); the residues are the same bits as the block's.
-template <class Reg>
-__device__ __noinline__ void reg_replay8(u64 r, u32 n0, typename Reg::K X, WalkOut o) {
-    for (u32 j = 0; j < 8; ++j) {
+// Replay N steps from r at n0 with exact tests (the PTX blocks saw a
+// possible hit in them); the residues are the same bits as the blocks'.
+template <class Reg, int N>
+__device__ __noinline__ void reg_replay(u64 r, u32 n0, typename Reg::K X, WalkOut o) {
+    for (u32 j = 0; j < N; ++j) {
         reg_check<Reg>(r, n0 + j, X, o);
         r = Reg::step(r, n0 + j + 1, X);
     }
+}
+template <class Reg>
+__device__ __forceinline__ void reg_replay8(u64 r, u32 n0, const typename Reg::K& X, const WalkOut& o) {
+    reg_replay<Reg, 8>(r, n0, X, o);
 }
 
 // Walk two candidates of one regime over [nstart, nend); residues in and out
@@ -337,8 +355,8 @@ __device__ __forceinline__ void walk_reg2(u64& ra, u64& rb, const typename Reg::
 template <class Reg>
 __device__ __forceinline__ void walk_reg_pair(u64& ra, u64& rb, const Prime& a, const Prime& b, bool real_b,
                                               u32 nstart, u32 nend, const WalkOut& o) {
-    const typename Reg::K A = Reg::make(a, nend);
-    const typename Reg::K B = real_b ? Reg::make(b, nend) : A;
+    const typename Reg::K A = Reg::make(a, nend, a.p);
+    const typename Reg::K B = real_b ? Reg::make(b, nend, b.p) : A;
     u64 wa = Reg::enter(ra, a, A);
     u64 wb = real_b ? Reg::enter(rb, b, B) : wa;
     walk_reg2<Reg>(wa, wb, A, B, real_b, nstart, nend, o);
@@ -360,14 +378,16 @@ __device__ __forceinline__ u64 walk_generic(u64 r, const Prime& c, u32 nstart, u
     return r;
 }
 
-// Walk regime of one candidate for multipliers up to kmax: 6 / 7 / 4 / 5 / 8
-// 32-bit / shifted-window 64-bit / lazy 64-bit / lazy 96-bit / canonical
-// 96-bit in half-offset form, 1 lazy 64-bit, 2 lazy 96-bit, 3 canonical
-// 96-bit, 0 generic Montgomery.
+// Walk regime of one candidate for multipliers up to kmax: 6 / 7 / 9 / 4 /
+// 5 / 8 32-bit / shifted-window 64-bit / 64-bit with the quotient on the
+// FP32 pipe / lazy 64-bit / lazy 96-bit / canonical 96-bit in half-offset
+// form, 1 lazy 64-bit, 2 lazy 96-bit, 3 canonical 96-bit, 0 generic
+// Montgomery.
 __device__ __forceinline__ int walk_regime(u64 p, u32 kmax) {
     if (half32_ok(p, kmax)) return 6;
     if (halfmid_ok(p, kmax)) return 7;
     if (canon96h_ok(p, kmax)) return 8;
+    if (halff_ok(p, kmax)) return 9;
     if (half_ok(p, kmax)) return 4;
     if (lazy_ok(p, kmax)) return 1;
     if (half96_ok(p, kmax)) return 5;
@@ -387,6 +407,7 @@ __device__ __forceinline__ void walk_one(u64& r, const Prime& c, int reg, u32 ns
         case 6: walk_reg_pair<RegH32>(r, dup, c, c, false, nstart, nend, o); break;
         case 7: walk_reg_pair<RegHM>(r, dup, c, c, false, nstart, nend, o); break;
         case 8: walk_reg_pair<RegC96H>(r, dup, c, c, false, nstart, nend, o); break;
+        case 9: walk_reg_pair<RegHF>(r, dup, c, c, false, nstart, nend, o); break;
         default: r = walk_generic(r, c, nstart, nend, o); break;
     }
 }
@@ -413,6 +434,7 @@ __device__ __forceinline__ void walk_pair(u64& ra, u64& rb, const Prime& a, cons
             case 6: walk_reg_pair<RegH32>(ra, rb, a, b, real_b, nstart, nend, o); return;
             case 7: walk_reg_pair<RegHM>(ra, rb, a, b, real_b, nstart, nend, o); return;
             case 8: walk_reg_pair<RegC96H>(ra, rb, a, b, real_b, nstart, nend, o); return;
+            case 9: walk_reg_pair<RegHF>(ra, rb, a, b, real_b, nstart, nend, o); return;
             default: walk_reg_pair<RegC96>(ra, rb, a, b, real_b, nstart, nend, o); return;
         }
     }
@@ -424,7 +446,8 @@ template <int WALK>
 __device__ __forceinline__ void walk_pair_as(u64& ra, u64& rb, const Prime& a, const Prime& b, bool real_b,
                                              u32 nstart, u32 nend, const WalkOut& o) {
     if (nstart >= nend) return;
-    if (WALK == WALK_H64) walk_reg_pair<RegH64>(ra, rb, a, b, real_b, nstart, nend, o);
+    if (WALK == WALK_HF) walk_reg_pair<RegHF>(ra, rb, a, b, real_b, nstart, nend, o);
+    else if (WALK == WALK_H64) walk_reg_pair<RegH64>(ra, rb, a, b, real_b, nstart, nend, o);
     else if (WALK == WALK_H96) walk_reg_pair<RegH96>(ra, rb, a, b, real_b, nstart, nend, o);
     else if (WALK == WALK_H32) walk_reg_pair<RegH32>(ra, rb, a, b, real_b, nstart, nend, o);
     else if (WALK == WALK_HM) walk_reg_pair<RegHM>(ra, rb, a, b, real_b, nstart, nend, o);
@@ -446,8 +469,10 @@ __device__ __forceinline__ void walk_pair_as(u64& ra, u64& rb, const Prime& a, c
 template <class Reg>
 __device__ __forceinline__ void walk_reg4(u64 (&r)[4], Prime (&c)[4], u32 nreal, u32 nstart, u32 nend,
                                           const WalkOut& o) {
-    const typename Reg::K K0 = Reg::make(c[0], nend), K1 = Reg::make(c[1], nend);
-    const typename Reg::K K2 = Reg::make(c[2], nend), K3 = Reg::make(c[3], nend);
+    // the thread's least candidate: one floor for all four keeps shared constants in shared registers
+    const u64 f = umin64(umin64(c[0].p, c[1].p), umin64(c[2].p, c[3].p));
+    const typename Reg::K K0 = Reg::make(c[0], nend, f), K1 = Reg::make(c[1], nend, f);
+    const typename Reg::K K2 = Reg::make(c[2], nend, f), K3 = Reg::make(c[3], nend, f);
     const u64 w0 = Reg::enter(r[0], c[0], K0), w1 = Reg::enter(r[1], c[1], K1);
     const u64 w2 = Reg::enter(r[2], c[2], K2), w3 = Reg::enter(r[3], c[3], K3);
     u32 l0 = (u32)w0, h0 = (u32)(w0 >> 32), l1 = (u32)w1, h1 = (u32)(w1 >> 32);
@@ -503,7 +528,8 @@ template <int WALK>
 __device__ __forceinline__ void walk_quad_as(u64 (&r)[4], Prime (&c)[4], u32 nreal, u32 nstart, u32 nend,
                                              const WalkOut& o) {
     if (nstart >= nend) return;
-    if (WALK == WALK_H64) walk_reg4<RegH64>(r, c, nreal, nstart, nend, o);
+    if (WALK == WALK_HF) walk_reg4<RegHF>(r, c, nreal, nstart, nend, o);
+    else if (WALK == WALK_H64) walk_reg4<RegH64>(r, c, nreal, nstart, nend, o);
     else if (WALK == WALK_H96) walk_reg4<RegH96>(r, c, nreal, nstart, nend, o);
     else if (WALK == WALK_H32) walk_reg4<RegH32>(r, c, nreal, nstart, nend, o);
     else if (WALK == WALK_HM) walk_reg4<RegHM>(r, c, nreal, nstart, nend, o);
@@ -522,6 +548,7 @@ __device__ __forceinline__ void walk_quad_as(u64 (&r)[4], Prime (&c)[4], u32 nre
 __device__ __forceinline__ void walk_quad_rt(int walk, u64 (&r)[4], Prime (&c)[4], u32 nreal, u32 nstart, u32 nend,
                                              const WalkOut& o) {
     switch (walk) {
+        case WALK_HF: walk_quad_as<WALK_HF>(r, c, nreal, nstart, nend, o); break;
         case WALK_H64: walk_quad_as<WALK_H64>(r, c, nreal, nstart, nend, o); break;
         case WALK_H96: walk_quad_as<WALK_H96>(r, c, nreal, nstart, nend, o); break;
         case WALK_H32: walk_quad_as<WALK_H32>(r, c, nreal, nstart, nend, o); break;

@@ -214,6 +214,11 @@ def test_hit_overflow_is_reported(ctx):
     ((1 << 36) - 150_000, (1 << 36) + 150_000, 2000, 2900),         # lazy / half-offset boundary at p = 2^36
     ((1 << 40) - 150_000, (1 << 40) + 150_000, 1_047_700, 1 << 20),    # p kmax = 2^60
     ((1 << 40) - 50_000, (1 << 40) + 50_000, 4_193_800, 1 << 22),      # half-offset 64-bit limit p kmax = 2^62
+    ((1 << 38) + 1, (1 << 38) + 300_001, 2000, 2900),               # float-quotient step at its floor p = 2^38
+    (10**12, 10**12 + 300_000, 441_000, 441_505),                  # float-quotient step at 19 k_max = 2^23
+    ((1 << 40) - 150_000, (1 << 40) + 150_000, 400_000, 400_700),  # float-quotient, threads on both sides of 2^40
+    ((1 << 50) - 200_000, 1 << 50, 3_500, 4096),                    # float-quotient step at p k_max = 2^62
+    ((1 << 56) - 200_000, (1 << 56) - 1, 40, 64),                   # float-quotient step, shift s - 32 = 20
 ])
 def test_walk_regimes_match_oracle(ctx, orc, lo, hi, nmin, nmax):
     """Every walk regime (and a pair straddling two) gives the oracle's residues, sums and hits."""

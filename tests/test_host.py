@@ -132,9 +132,10 @@ def test_context_needs_a_device(fslib):
 
 def test_walk_step_selection_boundaries(fslib):
     """The launch-wide step the host proves valid for a p-segment (fs_walk_step)."""
-    H64, T64, L96, C96, H96, H32, HM, C96H, ANY = 4, 1, 2, 3, 5, 6, 7, 8, 0
+    H64, T64, L96, C96, H96, H32, HM, C96H, HF, ANY = 4, 1, 2, 3, 5, 6, 7, 8, 9, 0
     ws = fslib.walk_step
-    assert ws(10**12, 10**12 + 10**8, 200_000) == H64                      # config 2
+    assert ws(10**12, 10**12 + 10**8, 200_000) == HF                       # config 2
+    assert ws(10**12, 10**12 + 10**9, 200_000) == HF                       # config 2, whole range
     assert ws(1 << 63, (1 << 63) + 10**9, 1_010_000) == C96H               # config 3
     assert ws(1 << 63, (1 << 63) + 10**9, 1 << 26) == C96                   # k_max >= 2^26 at p >= 2^63
     assert ws(10**6, 2 * 10**6, 2000) == H32                               # config 1: p < 2^31
@@ -145,6 +146,15 @@ def test_walk_step_selection_boundaries(fslib):
     assert ws(10**6, 2 * 10**6, 1 << 26) == ANY                             # k_max >= 2^26 at small p
     assert ws(1 << 36, (1 << 36) + 1000, 2000) == H64
     assert ws((1 << 36) - 1000, (1 << 36) + 1000, 2000) == T64              # straddles 2^36: the step valid on both sides
+    # float-quotient step: p >= 2^38, 19 kmax <= 2^23, 19 pmax kmax < 2^(bitlen(plo) + 23), p kmax <= 2^62
+    assert ws(1 << 38, (1 << 38) + 1000, 2000) == HF
+    assert ws((1 << 38) - 1000, (1 << 38) + 1000, 2000) == H64             # straddles 2^38
+    assert ws(10**12, 10**12 + 30_000, 441_505) == HF                       # 19 kmax <= 2^23
+    assert ws(10**12, 10**12 + 30_000, 441_506) == H64
+    assert ws((1 << 39) + 1, (1 << 40) - 1, 441_505) == HF                  # 19 pmax kmax < 2^63
+    assert ws((1 << 39) - 1000, (1 << 40) - 1, 441_505) == H64              # bitlen(plo) 39: z could reach 2^23
+    assert ws((1 << 50) - 10_000, (1 << 50) + 1, 4096) == HF                # p kmax = 2^62 exactly
+    assert ws((1 << 50) - 10_000, (1 << 50) + 2, 4096) == H96               # just above
     assert ws((1 << 35) + 1, (1 << 35) + 1000, 1 << 25) == T64              # 2^33 < p < 2^36, k_max >= 2^25
     k = 1 << 20
     assert ws(1 << 40, (1 << 40) + 1, k) == H64                             # p kmax = 2^60
@@ -178,5 +188,5 @@ def test_c_caller(fslib, tmp_path):
     assert (rc, kept, disc, first) == ("0", "2", "0", "149")          # sorted by (p, |n|), both kept
     assert int(cs) == (25 - 1) + (169725 + 1)                          # checksum += n + c per kept factor
     assert int(got["capacity"]) == fslib.candidate_capacity(10**12, 10**12 + 10**8)
-    assert got["walk_step"] == "4 6"
+    assert got["walk_step"] == "9 6"
     assert got["strerror"].strip() == fslib.lib().fs_strerror(fslib.FS_E_OVERFLOW).decode()
