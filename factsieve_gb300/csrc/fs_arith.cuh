@@ -582,10 +582,10 @@ __device__ __forceinline__ u64 halff_step(u64 r, u32 k, const HalfF& H) {
 }
 __device__ __forceinline__ u64 halff_canon(u64 r, const HalfF& H) { return r >= H.p ? r - H.p : r; }
 
-#define FS_HFF_MUL(RL, RH, NP0, NP1, MF, SH, HC, T, R, TL, TH, Q, Z, F) \
-    "mul.wide.u32 " T ", " RL ", kk;\n\t"                                \
-    "mov.b64 {" TL ", " TH "}, " T ";\n\t"                               \
-    "mad.lo.u32 " TH ", " RH ", kk, " TH ";\n\t"                         \
+#define FS_HFF_MUL(RL, RH, NP0, NP1, MF, SH, HC, T, R, TL, TH, Q, Z, F, KK) \
+    "mul.wide.u32 " T ", " RL ", " KK ";\n\t"                                \
+    "mov.b64 {" TL ", " TH "}, " T ";\n\t"                                   \
+    "mad.lo.u32 " TH ", " RH ", " KK ", " TH ";\n\t"                         \
     "shf.r.wrap.b32 " Z ", " TH ", " HC ", " SH ";\n\t"                  \
     "mov.b32 " F ", " Z ";\n\t"                                          \
     "sub.rn.f32 " F ", " F ", 0f20000000;\n\t"                           \
@@ -595,12 +595,13 @@ __device__ __forceinline__ u64 halff_canon(u64 r, const HalfF& H) { return r >= 
     "mad.wide.u32 " R ", " Q ", " NP0 ", " T ";\n\t"                     \
     "mov.b64 {" RL ", " RH "}, " R ";\n\t"                               \
     "mad.lo.u32 " RH ", " Q ", " NP1 ", " RH ";\n\t"
-#define FS_HFF_STEP2(J)                                                                              \
-    "add.u32 kk, %5, " #J ";\n\t"                                                                    \
+// The multipliers k1 .. k1 + 7 come in as operands %20-%27: computed outside
+// the asm, they are shared by the blocks of a thread's two pairs.
+#define FS_HFF_STEP2(KK)                                                                             \
     FS_HF_TEST("%0", "%9", "%10")                                                                    \
     FS_HF_TEST("%2", "%16", "%17")                                                                   \
-    FS_HFF_MUL("%0", "%1", "%6", "%7", "%8", "%11", "%12", "TA", "RA", "aL", "aH", "qA", "zA", "fA") \
-    FS_HFF_MUL("%2", "%3", "%13", "%14", "%15", "%18", "%19", "TB", "RB", "bL", "bH", "qB", "zB", "fB")
+    FS_HFF_MUL("%0", "%1", "%6", "%7", "%8", "%11", "%12", "TA", "RA", "aL", "aH", "qA", "zA", "fA", KK) \
+    FS_HFF_MUL("%2", "%3", "%13", "%14", "%15", "%18", "%19", "TB", "RB", "bL", "bH", "qB", "zB", "fB", KK)
 
 // Eight float-quotient half-offset steps on two residues; the flag as
 // lazy_walk8x2's.
@@ -608,18 +609,19 @@ __device__ __forceinline__ u32 halff_walk8x2(u32& al, u32& ah, u32& bl, u32& bh,
                                              const HalfF& B) {
     u32 flag;
     asm("{\n\t"
-        ".reg .u32 kk, aL, aH, qA, zA, bL, bH, qB, zB;\n\t"
+        ".reg .u32 aL, aH, qA, zA, bL, bH, qB, zB;\n\t"
         ".reg .f32 fA, fB;\n\t"
         ".reg .u64 TA, RA, TB, RB;\n\t"
         ".reg .pred P;\n\t"
         "setp.ne.u32 P, %5, %5;\n\t"
-        FS_HFF_STEP2(0) FS_HFF_STEP2(1) FS_HFF_STEP2(2) FS_HFF_STEP2(3)
-        FS_HFF_STEP2(4) FS_HFF_STEP2(5) FS_HFF_STEP2(6) FS_HFF_STEP2(7)
+        FS_HFF_STEP2("%20") FS_HFF_STEP2("%21") FS_HFF_STEP2("%22") FS_HFF_STEP2("%23")
+        FS_HFF_STEP2("%24") FS_HFF_STEP2("%25") FS_HFF_STEP2("%26") FS_HFF_STEP2("%27")
         "selp.u32 %4, 1, 0, P;\n\t"
         "}"
         : "+r"(al), "+r"(ah), "+r"(bl), "+r"(bh), "=r"(flag)
         : "r"(k1), "r"(A.np0), "r"(A.np1), "f"(A.mf), "r"(A.x0), "r"(A.x1), "r"(A.sh), "r"(A.hc),
-          "r"(B.np0), "r"(B.np1), "f"(B.mf), "r"(B.x0), "r"(B.x1), "r"(B.sh), "r"(B.hc));
+          "r"(B.np0), "r"(B.np1), "f"(B.mf), "r"(B.x0), "r"(B.x1), "r"(B.sh), "r"(B.hc),
+          "r"(k1), "r"(k1 + 1), "r"(k1 + 2), "r"(k1 + 3), "r"(k1 + 4), "r"(k1 + 5), "r"(k1 + 6), "r"(k1 + 7));
     return flag;
 }
 
