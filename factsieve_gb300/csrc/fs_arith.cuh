@@ -517,9 +517,9 @@ __device__ __forceinline__ u32 half_walk8x2(u32& al, u32& ah, u32& bl, u32& bh, 
 // 1 + 2^s/p + (t/p) 2^-23, which is below 1 + 1/8 + 1/16 when
 // r < (19/16) p and 19 k_max <= 2^23.  So r stays below (19/16) p < x + p,
 // and the exact test is r in {x, x + 1}, as in the half-offset lazy step.
-// Validity over a launch, with f the thread's least candidate: p >= 2^38,
-// p k_max <= 2^62, 19 k_max <= 2^23, and 19 p_max k_max <
-// 2^(bitlen(p_min) + 23), which keeps z < 2^23.  The two float instructions
+// Validity over a launch (checked by the host, walk_for_range), with f the
+// thread's least candidate: p >= 2^38, p k_max <= 2^62, 19 k_max <= 2^23,
+// and 19 p_max k_max < 2^(bitlen(p_min) + 23), which keeps z < 2^23.  The two float instructions
 // have no .ftz, so subnormals are kept.
 struct HalfF {
     u64 p, x;
@@ -528,14 +528,6 @@ struct HalfF {
     u32 sh, hc;               // s - 32 and 2^(s - 35): the funnel shift that builds F
     u32 x0, x1;               // low words of x and x + 1
 };
-
-__device__ __forceinline__ bool halff_ok(u64 p, u32 kmax) {
-    if (p < (1ull << 38) || kmax == 0 || 19ull * kmax > (1ull << 23) || p > (1ull << 62) / kmax) return false;
-    const u64 v = p * (u64)kmax;                       // exact: p kmax <= 2^62
-    const u64 hi = __umul64hi(v, 19ull), lo = v * 19ull;
-    const int e = bitlen64(p) + 23;                    // 19 p k_max < 2^e
-    return e >= 64 ? (hi >> (e - 64)) == 0 : (hi == 0 && (lo >> e) == 0);
-}
 
 // f <= p: the floor that sets s (the least candidate of the thread, whose
 // launch-wide validity the host has shown, or p itself).

@@ -430,8 +430,9 @@ int walk_for_range(uint64_t plo, uint64_t phi, uint32_t kmax) {
     // the shifted-window half-offset step needs 2^31 <= p < 2^36 and kmax < 2^25 (halfmid_ok)
     if (plo >= (1ull << 31) && pmax < (1ull << 36) && kb <= 25) return WALK_HM;
     // the float-quotient half-offset step needs p >= 2^38, p kmax <= 2^62,
-    // 19 kmax <= 2^23 and 19 pmax kmax < 2^(bitlen(plo) + 23) (halff_ok, with
-    // s taken from a thread's least candidate)
+    // 19 kmax <= 2^23 and 19 pmax kmax < 2^(bitlen(plo) + 23) (the bounds
+    // of halff_walk8x2 with s taken from a thread's least candidate; launch-
+    // wide only, no per-candidate test)
     if (plo >= (1ull << 38) && pmax <= ((1ull << 62) / kmax) && 19ull * kmax <= (1ull << 23) &&
         (unsigned __int128)19 * pmax * kmax < ((unsigned __int128)1 << ((64 - __builtin_clzll(plo)) + 23)))
         return WALK_HF;

@@ -378,16 +378,16 @@ __device__ __forceinline__ u64 walk_generic(u64 r, const Prime& c, u32 nstart, u
     return r;
 }
 
-// Walk regime of one candidate for multipliers up to kmax: 6 / 7 / 9 / 4 /
-// 5 / 8 32-bit / shifted-window 64-bit / 64-bit with the quotient on the
-// FP32 pipe / lazy 64-bit / lazy 96-bit / canonical 96-bit in half-offset
-// form, 1 lazy 64-bit, 2 lazy 96-bit, 3 canonical 96-bit, 0 generic
-// Montgomery.
+// Walk regime of one candidate for multipliers up to kmax: 6 / 7 / 4 / 5 / 8
+// 32-bit / shifted-window 64-bit / lazy 64-bit / lazy 96-bit / canonical
+// 96-bit in half-offset form, 1 lazy 64-bit, 2 lazy 96-bit, 3 canonical
+// 96-bit, 0 generic Montgomery.  (The float-quotient step runs only where
+// the host has shown it valid for a whole launch: per candidate it would
+// add little and cost the mixed-step kernel registers.)
 __device__ __forceinline__ int walk_regime(u64 p, u32 kmax) {
     if (half32_ok(p, kmax)) return 6;
     if (halfmid_ok(p, kmax)) return 7;
     if (canon96h_ok(p, kmax)) return 8;
-    if (halff_ok(p, kmax)) return 9;
     if (half_ok(p, kmax)) return 4;
     if (lazy_ok(p, kmax)) return 1;
     if (half96_ok(p, kmax)) return 5;
@@ -407,7 +407,6 @@ __device__ __forceinline__ void walk_one(u64& r, const Prime& c, int reg, u32 ns
         case 6: walk_reg_pair<RegH32>(r, dup, c, c, false, nstart, nend, o); break;
         case 7: walk_reg_pair<RegHM>(r, dup, c, c, false, nstart, nend, o); break;
         case 8: walk_reg_pair<RegC96H>(r, dup, c, c, false, nstart, nend, o); break;
-        case 9: walk_reg_pair<RegHF>(r, dup, c, c, false, nstart, nend, o); break;
         default: r = walk_generic(r, c, nstart, nend, o); break;
     }
 }
@@ -434,7 +433,6 @@ __device__ __forceinline__ void walk_pair(u64& ra, u64& rb, const Prime& a, cons
             case 6: walk_reg_pair<RegH32>(ra, rb, a, b, real_b, nstart, nend, o); return;
             case 7: walk_reg_pair<RegHM>(ra, rb, a, b, real_b, nstart, nend, o); return;
             case 8: walk_reg_pair<RegC96H>(ra, rb, a, b, real_b, nstart, nend, o); return;
-            case 9: walk_reg_pair<RegHF>(ra, rb, a, b, real_b, nstart, nend, o); return;
             default: walk_reg_pair<RegC96>(ra, rb, a, b, real_b, nstart, nend, o); return;
         }
     }
