@@ -92,15 +92,22 @@ STEP_CEILING_KIND = {6: (11, "32-bit half-offset step"), 7: (12, "shifted-window
                      0: (9, "generic Montgomery step")}
 
 
-def setup_products(fs, nmin: int) -> int:
-    """Montgomery products per candidate outside the walk: the bit-layered plan
-    (one per word, one squaring per layer after the first), the R^(D+1)
-    correction (square-and-multiply over the deficit D), the constants R mod p
-    and R^2 mod p (five squarings, built twice for four-candidate threads),
-    entering and leaving the walk's residue form and the final nmax check."""
+def setup_products(fs, nmin: int, folded: bool = False):
+    """Products per candidate outside the walk, as (plan products, other
+    Montgomery products).  The bit-layered plan costs one product per word and
+    one squaring per layer after the first; with Montgomery products the
+    R^(D+1) correction (square-and-multiply over the deficit D) follows, while
+    the folding products modulo 2^63 + d (folded=True) have no deficit but
+    double by a product (one per doubling layer) and end with one conversion
+    to Montgomery form.  Both add the constants R mod p and R^2 mod p (five
+    squarings, built twice for four-candidate threads), entering and leaving
+    the walk's residue form and the final nmax check."""
     words, layers, deficit = fs.setup_plan(nmin)
+    plan = len(words) + max(len(layers) - 1, 0)
+    if folded:
+        return plan + int(sum(int(l[2]) for l in layers)), 1 + 10 + 2 + 3
     pow_d = max(int(deficit).bit_length() - 1, 0) + bin(int(deficit)).count("1")
-    return len(words) + max(len(layers) - 1, 0) + pow_d + 1 + 10 + 2 + 3
+    return plan, pow_d + 1 + 10 + 2 + 3
 
 
 def roofline(ctx, fs, wl, ncand, st, step_ms, clocks=None, seg=None):
@@ -108,9 +115,9 @@ def roofline(ctx, fs, wl, ncand, st, step_ms, clocks=None, seg=None):
     multiplication: integer multiply-add, no memory traffic to speak of (the
     candidate list is read once).  The ceiling is the same arithmetic run
     register-resident at full occupancy on this GPU (fs_bench_int_pipe kinds
-    4-13: the walk's own PTX step blocks and the Montgomery product), so
-    peak = pair-steps the kernel would finish if its walk ran at the walk
-    ceiling and its setup at the Montgomery-product ceiling."""
+    4-15: the walk's own PTX step blocks, the Montgomery product and the
+    folding product), so peak = pair-steps the kernel would finish if its walk
+    ran at the walk ceiling and its setup products at their ceilings."""
     pmin, pmax, nmin, nmax, seg0 = WORKLOADS[wl]
     seg = seg or seg0
     W = nmax - nmin
@@ -119,11 +126,14 @@ def roofline(ctx, fs, wl, ncand, st, step_ms, clocks=None, seg=None):
     walk_ceil, _ = ctx.bench_int_pipe(kind, 4000)
     mm_ceil, _ = ctx.bench_int_pipe(4, 4000)
     imad_ops, _ = ctx.bench_int_pipe(0, 20000)
-    smp = setup_products(fs, nmin)
+    folded = bool(fs.setup_form(pmin, min(pmin + seg, pmax))) and step in (3, 8)
+    plan_ceil = ctx.bench_int_pipe(15, 4000)[0] if folded else mm_ceil
+    plan_products, mont_products = setup_products(fs, nmin, folded)
+    smp = plan_products + mont_products
     sieve_s = st["sieve_ms"] * 1e-3
     launches = max(st["sieve_launches"], 1)
     pairs = ncand * W
-    lower_bound_s = ncand * (W / walk_ceil + smp / mm_ceil)
+    lower_bound_s = ncand * (W / walk_ceil + plan_products / plan_ceil + mont_products / mm_ceil)
     achieved = pairs / sieve_s if sieve_s > 0 else 0.0
     peak = pairs / lower_bound_s if lower_bound_s > 0 else 0.0
     cap = NCU_CAPTURE.get(wl, {})
@@ -151,10 +161,11 @@ def roofline(ctx, fs, wl, ncand, st, step_ms, clocks=None, seg=None):
         "share_of_step": st["sieve_ms"] / step_ms if step_ms else None,
         "walk_step": step_name,
         "ceilings": {"walk_steps_per_s": walk_ceil, "montgomery_products_per_s": mm_ceil,
-                     "imad_lane_ops_per_s": imad_ops},
+                     "plan_products_per_s": plan_ceil, "imad_lane_ops_per_s": imad_ops},
         "setup_products_per_candidate": smp,
+        "setup_product": "folding modulo 2^63 + d" if folded else "Montgomery",
         "peak_source": "measured on this GPU: the walk step's PTX block and mont_mul, register-resident at full "
-                       "occupancy (fs_bench_int_pipe kinds 4-14)",
+                       "occupancy (fs_bench_int_pipe kinds 4-15)",
         "imad_pipe_busy_ncu": cap.get("imad_pipe_busy"), "ncu_source": cap.get("source"),
         "hbm": {"achieved": hbm_ach, "peak": hbm_peak, "unit": "GB/s",
                 "frac": hbm_ach / hbm_peak if hbm_peak else None,

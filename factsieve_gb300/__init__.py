@@ -104,6 +104,7 @@ def _declare(L):
         "fs_bench_int_pipe": (C.c_int, [vp, u32, u32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
         "fs_search_pending": (C.c_int, [vp, P64]),
         "fs_walk_step": (C.c_int, [u64, u64, u32]),
+        "fs_setup_form": (C.c_int, [u64, u64]),
         "fs_set_timing": (C.c_int, [vp, C.c_int]),
         "fs_get_stats": (C.c_int, [vp, C.POINTER(Stats)]),
         "fs_reset_stats": (C.c_int, [vp]),
@@ -196,10 +197,18 @@ def setup_plan_chunks(n: int, chunks: int):
 
 def walk_step(plo: int, phi: int, kmax: int) -> int:
     """The residue step the sieve runs for p in [plo, phi), multipliers up to kmax
-    (6 / 7 / 4 / 5 / 8 half-offset 32-bit / shifted-window 64-bit / lazy 64-bit /
-    lazy 96-bit / canonical 96-bit, 1 lazy 64-bit, 2 lazy 96-bit, 3 canonical
-    96-bit, 0 chosen per candidate)."""
+    (6 / 7 / 9 / 4 / 5 / 8 half-offset 32-bit / shifted-window 64-bit / 64-bit
+    with the quotient on the FP32 pipe / lazy 64-bit / lazy 96-bit / canonical
+    96-bit, 1 lazy 64-bit, 2 lazy 96-bit, 3 canonical 96-bit, 0 chosen per
+    candidate)."""
     return int(lib().fs_walk_step(plo, phi, kmax))
+
+
+def setup_form(plo: int, phi: int) -> int:
+    """1 when the setup of p in [plo, phi) folds its products modulo 2^63 + d
+    (every p = 2^63 + d with 0 < d < 2^30; four-candidate kernels, 96-bit walks),
+    else 0 (Montgomery products)."""
+    return int(lib().fs_setup_form(plo, phi))
 
 
 def find_wheel_offset(start: int):

@@ -42,8 +42,9 @@ __device__ __forceinline__ u64 inv64(u64 p) {
 // (a*b - m*p)/R with m = (a*b mod R)*p^-1: the low halves cancel exactly,
 // the high halves differ by less than p, one conditional add folds it.
 __device__ __forceinline__ u64 mont_mul(u64 a, u64 b, u64 p, u64 pinv) {
-    u64 lo = a * b;
-    u64 hi = mulhi64(a, b);
+    const unsigned __int128 x = (unsigned __int128)a * b;
+    u64 lo = (u64)x;
+    u64 hi = (u64)(x >> 64);
     u64 m = lo * pinv;
     u64 mp = mulhi64(m, p);
     u64 r = hi - mp;
@@ -93,6 +94,51 @@ __device__ __forceinline__ u64 mont_pow(u64 base, u64 e, const Prime& c) {
     }
     return a;
 }
+
+// ----------------- setup: products modulo p = 2^63 + d, 0 < d < 2^30 --
+//
+// For p just above 2^63, 2^64 = 2p - 2d, so 2^64 = -e (mod p) with e = 2d
+// < 2^31, and a product folds down without Montgomery's second wide product:
+//   x = a b = X1 2^64 + X0            = X0 - e X1
+//   W = e X1 = W1 2^64 + W0 (W1 < e)  = W0 - e W1
+//   u = X0 - W0 = u' - b 2^64         = u' + b e      (b the borrow)
+// so a b = u' + e (W1 + b) (mod p), where e (W1 + b) < 2^62.  If that
+// last sum carries out of 64 bits, its value is y' + 2^64 = y' + (p - e),
+// and y' + p - e < 2^64.  The result is a 64-bit value congruent to a b,
+// for any 64-bit a and b (lazy: pm_canon makes it canonical).  Cost: one
+// full 64x64->128 product and three 32x32->64 ones, against the Montgomery
+// product's full product, 64x64 low product and 64x64 high product.
+struct PMod {
+    u32 e;          // 2d
+    u32 pe0, pe1;   // p - e = 2^63 - d, two words
+};
+
+__device__ __forceinline__ PMod make_pmod(u64 p) {
+    PMod m;
+    const u64 d = p - (1ull << 63);
+    m.e = (u32)(d << 1);
+    const u64 pe = p - 2 * d;
+    m.pe0 = (u32)pe;
+    m.pe1 = (u32)(pe >> 32);
+    return m;
+}
+
+__device__ __forceinline__ u64 pm_mul(u64 a, u64 b, const PMod& m) {
+    const unsigned __int128 x = (unsigned __int128)a * b;
+    const u64 x0 = (u64)x, x1 = (u64)(x >> 64);                     // a b = x1 2^64 + x0
+    const u64 t0 = (u64)m.e * (u32)x1;
+    const u64 t1 = (u64)m.e * (u32)(x1 >> 32) + (t0 >> 32);         // e x1 = (t1 >> 32) 2^64 + w0
+    const u64 w0 = (t1 << 32) | (u32)t0;
+    const u64 u = x0 - w0;
+    const u32 w1b = (u32)(t1 >> 32) + (x0 < w0 ? 1u : 0u);         // W1 + borrow < 2^31
+    const u64 v = (u64)m.e * w1b;                                    // < 2^62
+    const u64 y = u + v;
+    const u64 pe = ((u64)m.pe1 << 32) | m.pe0;
+    return y < u ? y + pe : y;                                       // a carry out: + (p - e)
+}
+
+// The canonical residue of a pm_mul result (< 2^64 < 2p).
+__device__ __forceinline__ u64 pm_canon(u64 y, u64 p) { return y >= p ? y - p : y; }
 
 // Base-2 strong probable-prime test of odd n > 2 (the candidate filter of
 // kernels/getsegprimes.cl:79-108): 2^d by a left-to-right ladder whose

@@ -327,7 +327,13 @@ int run_sieve(fs_ctx* c, const u64* d_cand, uint32_t cap, fs::Counters* d_ctr, u
         std::pair<cudaEvent_t, cudaEvent_t> ev;
         if ((rc = ev_begin(c, &ev))) return rc;
         const int kv = kernel_variant(variant(c), walk);
-        CK(c, fs::launch_sieve(a, first ? setup_mode : fs::SETUP_LOAD, fin, sieve_grid(c, kv), c->stream, kv, walk));
+        int smode = first ? setup_mode : fs::SETUP_LOAD;
+        // p = 2^63 + d, d < 2^30 over the segment: the four-candidate kernels of
+        // the 96-bit walks fold their setup products instead of Montgomery's
+        if (smode == fs::SETUP_PLAN && kv == 5 && (walk == fs::WALK_C96H || walk == fs::WALK_C96) &&
+            fs::pm_setup_for_range(plo, phi))
+            smode = fs::SETUP_PLAN_PM;
+        CK(c, fs::launch_sieve(a, smode, fin, sieve_grid(c, kv), c->stream, kv, walk));
         if ((rc = ev_end(c, ev, c->sieve_ev))) return rc;
         ++c->launches;
         ++c->sieve_launches;
@@ -746,9 +752,10 @@ int fs_plan_check(fs_ctx* c, const uint64_t* d_cand, fs_counters* d_ctr, uint32_
 }
 
 int fs_walk_step(uint64_t plo, uint64_t phi, uint32_t kmax) { return fs::walk_for_range(plo, phi, kmax); }
+int fs_setup_form(uint64_t plo, uint64_t phi) { return fs::pm_setup_for_range(plo, phi); }
 
 int fs_bench_int_pipe(fs_ctx* c, uint32_t kind, uint32_t iters, double* ops_per_sec, double* ms) {
-    if (!c || kind > 14 || iters == 0 || iters > (1u << 24)) return FS_E_ARG;
+    if (!c || kind > 15 || iters == 0 || iters > (1u << 24)) return FS_E_ARG;
     int rc = bind(c);
     if (rc) return rc;
     const int grid = c->sm_count * 8;   // 8 x 256 threads = 2048 per SM

@@ -247,7 +247,8 @@ __global__ void __launch_bounds__(256) imad_bench_kernel(u32 iters, u32 kind, u3
 //   kind 12 shifted-window half-offset 64-bit steps (halfmid_walk8x2), 4 chains
 //   kind 13 half-offset canonical 96-bit steps (canon96h_walk8x2), 4 chains
 //   kind 14 half-offset 64-bit steps, quotient on the FP32 pipe (halff_walk8x2), 4 chains
-constexpr u32 kCeilUnits[15] = {0, 0, 0, 0, 8, 32, 32, 32, 32, 4, 32, 32, 32, 32, 32};
+//   kind 15 folding products modulo p = 2^63 + d (pm_mul), 8 chains
+constexpr u32 kCeilUnits[16] = {0, 0, 0, 0, 8, 32, 32, 32, 32, 4, 32, 32, 32, 32, 32, 8};
 
 template <u32 kind>
 __global__ void __launch_bounds__(256) ceiling_kernel(u32 iters, u32 seed, u32* sink) {
@@ -271,7 +272,23 @@ __global__ void __launch_bounds__(256) ceiling_kernel(u32 iters, u32 seed, u32* 
     for (int h = 0; h < 4; ++h) c[h] = make_prime((base + 2ull * (4ull * tid + h) + 2ull * seed) | 1ull);
     const u32 k0 = 100001;   // multipliers k0 .. k0 + 8 iters: below 2^28 and p k below each regime's bound
     u32 acc = 0;
-    if constexpr (kind == 4) {
+    if constexpr (kind == 15) {
+        // moduli 2^63 + d with d < 2^30: base + 2 (4 tid + h) + 2 seed stays below 2^63 + 2^30
+        // for the grids of fs_bench_int_pipe (8 blocks of 256 threads per SM)
+        u64 x[8];
+        PMod m[4];
+#pragma unroll
+        for (int h = 0; h < 4; ++h) m[h] = make_pmod(c[h].p);
+#pragma unroll
+        for (int h = 0; h < 8; ++h) x[h] = c[h & 3].one + h;
+        const u64 y = c[0].r2;
+        for (u32 it = 0; it < iters; ++it) {
+#pragma unroll
+            for (int h = 0; h < 8; ++h) x[h] = pm_mul(x[h], y, m[h & 3]);
+        }
+#pragma unroll
+        for (int h = 0; h < 8; ++h) acc ^= (u32)x[h] ^ (u32)(x[h] >> 32);
+    } else if constexpr (kind == 4) {
         u64 x[8];
 #pragma unroll
         for (int h = 0; h < 8; ++h) x[h] = c[h & 3].one + h;
@@ -414,12 +431,13 @@ cudaError_t launch_imad_bench(u32 iters, u32 kind, u32 seed, u32* sink, int grid
         case 12: ceiling_kernel<12><<<grid, 256, 0, s>>>(iters, seed, sink); break;
         case 13: ceiling_kernel<13><<<grid, 256, 0, s>>>(iters, seed, sink); break;
         case 14: ceiling_kernel<14><<<grid, 256, 0, s>>>(iters, seed, sink); break;
+        case 15: ceiling_kernel<15><<<grid, 256, 0, s>>>(iters, seed, sink); break;
         default: imad_bench_kernel<<<grid, 256, 0, s>>>(iters, kind, seed, sink); break;
     }
     return cudaGetLastError();
 }
 
-double bench_units_per_thread_iter(u32 kind) { return kind < 4 ? 8.0 : (kind < 15 ? kCeilUnits[kind] : 0.0); }
+double bench_units_per_thread_iter(u32 kind) { return kind < 4 ? 8.0 : (kind < 16 ? kCeilUnits[kind] : 0.0); }
 
 int walk_for_range(uint64_t plo, uint64_t phi, uint32_t kmax) {
     if (phi <= plo || kmax == 0) return WALK_ANY;
@@ -449,6 +467,12 @@ int walk_for_range(uint64_t plo, uint64_t phi, uint32_t kmax) {
     if (kb <= 26 && (plo >> 63) != 0) return WALK_C96H;
     if (kb <= 28 && (plo >> 63) != 0) return WALK_C96;
     return WALK_ANY;
+}
+
+int pm_setup_for_range(uint64_t plo, uint64_t phi) {
+    // candidates are odd, so p >= 2^63 means d >= 1
+    if (phi <= plo) return 0;
+    return plo >= (1ull << 63) && phi - 1 < (1ull << 63) + (1ull << 30) ? 1 : 0;
 }
 
 int sieve_threads() { return kSieveThreads; }

@@ -7,7 +7,10 @@
 
 namespace fs {
 
-enum { SETUP_LOAD = 0, SETUP_PLAN = 1, SETUP_PARTIALS = 2 };
+// SETUP_PLAN_PM: SETUP_PLAN for a launch whose candidates all lie in
+// (2^63, 2^63 + 2^30), with the folding product of that form (four
+// candidates per thread, 96-bit walks only).
+enum { SETUP_LOAD = 0, SETUP_PLAN = 1, SETUP_PARTIALS = 2, SETUP_PLAN_PM = 3 };
 // Walk step used for every candidate of a launch (WALK_ANY: per candidate).
 enum { WALK_ANY = 0, WALK_T64 = 1, WALK_L96 = 2, WALK_C96 = 3, WALK_H64 = 4, WALK_H96 = 5, WALK_H32 = 6, WALK_HM = 7,
        WALK_C96H = 8, WALK_HF = 9 };
@@ -130,6 +133,9 @@ cudaError_t sieve_pair_occupancy(int* blocks_per_sm);
 cudaError_t sieve_quad_occupancy(int* blocks_per_sm);
 // The walk step valid for every p in [plo, phi) with multipliers up to kmax.
 int walk_for_range(uint64_t plo, uint64_t phi, uint32_t kmax);
+// 1 when every odd p in [plo, phi) has the form 2^63 + d with 0 < d < 2^30
+// (the setup's folding product applies), else 0.
+int pm_setup_for_range(uint64_t plo, uint64_t phi);
 cudaError_t launch_setup_partial(const SieveArgs& a, int grid_x, int nchunks, cudaStream_t s);
 cudaError_t launch_table_check(const TableCheckArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_imad_bench(u32 iters, u32 kind, u32 seed, u32* sink, int grid, cudaStream_t s);

@@ -7,7 +7,7 @@ namespace fs {
 template <int MINB, int WALK, int PPT = 2>
 static void launch_sieve_w(const SieveArgs& a, int setup, bool fin, int grid, cudaStream_t s) {
     const int t = kSieveThreads;
-    if (setup == SETUP_PLAN) {
+    if (setup == SETUP_PLAN || setup == SETUP_PLAN_PM) {   // the pair kernels take every plan with Montgomery products
         if (fin) sieve_kernel<SETUP_PLAN, true, MINB, WALK, PPT><<<grid, t, 0, s>>>(a);
         else sieve_kernel<SETUP_PLAN, false, MINB, WALK, PPT><<<grid, t, 0, s>>>(a);
     } else if (setup == SETUP_PARTIALS) {

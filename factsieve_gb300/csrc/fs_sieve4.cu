@@ -7,7 +7,14 @@ namespace fs {
 template <int MINB, int WALK, int PPT = 2>
 static void launch_sieve_w(const SieveArgs& a, int setup, bool fin, int grid, cudaStream_t s) {
     const int t = kSieveThreads;
-    if (setup == SETUP_PLAN) {
+    if constexpr (WALK == WALK_C96H || WALK == WALK_C96) {
+        if (setup == SETUP_PLAN_PM) {
+            if (fin) sieve_kernel<SETUP_PLAN_PM, true, MINB, WALK, PPT><<<grid, t, 0, s>>>(a);
+            else sieve_kernel<SETUP_PLAN_PM, false, MINB, WALK, PPT><<<grid, t, 0, s>>>(a);
+            return;
+        }
+    }
+    if (setup == SETUP_PLAN || setup == SETUP_PLAN_PM) {
         if (fin) sieve_kernel<SETUP_PLAN, true, MINB, WALK, PPT><<<grid, t, 0, s>>>(a);
         else sieve_kernel<SETUP_PLAN, false, MINB, WALK, PPT><<<grid, t, 0, s>>>(a);
     } else if (setup == SETUP_PARTIALS) {

@@ -166,6 +166,56 @@ __device__ __forceinline__ void plan_product4(const Prime (&c)[4], const u64* __
     }
 }
 
+// plan_product4 for p = 2^63 + d (0 < d < 2^30) with the folding product
+// pm_mul in place of Montgomery's: plain residues from 1, no R^-1 deficit;
+// x[h] ends as n! mod p, lazy (any 64-bit value congruent to it).
+__device__ __forceinline__ void plan_product4_pm(const Prime (&c)[4], const u64* __restrict__ words,
+                                                 const Layer* __restrict__ layers, u32 lb, u32 le, u64 (&x)[4]) {
+    PMod m[4];
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+        m[h] = make_pmod(c[h].p);
+        x[h] = 1;
+    }
+    for (u32 l = lb; l < le; ++l) {
+        const Layer L = layers[l];
+        if (l != lb) {
+#pragma unroll
+            for (int h = 0; h < 4; ++h) x[h] = pm_mul(x[h], x[h], m[h]);
+        }
+        if (L.dbl) {
+#pragma unroll
+            for (int h = 0; h < 4; ++h) x[h] = pm_mul(x[h], 2, m[h]);
+        }
+        u32 i = L.begin;
+        if ((i & 1) && i < L.end) {
+            const u64 w = __ldg(words + i++);
+#pragma unroll
+            for (int h = 0; h < 4; ++h) x[h] = pm_mul(x[h], w, m[h]);
+        }
+        if (i + 2 <= L.end) {
+            u64 y[4];
+#pragma unroll
+            for (int h = 0; h < 4; ++h) y[h] = 1;
+            for (; i + 2 <= L.end; i += 2) {
+                const ulonglong2 w2 = __ldg(reinterpret_cast<const ulonglong2*>(words + i));
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                    x[h] = pm_mul(x[h], w2.x, m[h]);
+                    y[h] = pm_mul(y[h], w2.y, m[h]);
+                }
+            }
+#pragma unroll
+            for (int h = 0; h < 4; ++h) x[h] = pm_mul(x[h], y[h], m[h]);
+        }
+        if (i < L.end) {
+            const u64 w = __ldg(words + i);
+#pragma unroll
+            for (int h = 0; h < 4; ++h) x[h] = pm_mul(x[h], w, m[h]);
+        }
+    }
+}
+
 struct WalkOut {
     HitStage* st;
     Factor* hits;
@@ -619,11 +669,16 @@ __global__ void __launch_bounds__(kSieveThreads, MINB) sieve_kernel(SieveArgs a)
 #pragma unroll
             for (int h = 1; h < 4; ++h) c[h] = (u32)h < nreal ? make_prime(a.cand[i0 + h]) : c[0];
             u64 r[4];
-            if (SETUP == SETUP_PLAN) {
+            if constexpr (SETUP == SETUP_PLAN) {
                 plan_product4(c, a.plan.words, a.plan.layers, a.plan.layer_begin, a.plan.layer_end, r);
 #pragma unroll
                 for (int h = 0; h < 4; ++h)
                     r[h] = mont_mul(r[h], mont_pow(c[h].r2, a.plan.deficit, c[h]), c[h].p, c[h].pinv);
+            } else if constexpr (SETUP == SETUP_PLAN_PM) {
+                // p = 2^63 + d, d < 2^30 over the launch, one plan chunk: plain n! mod p, then n! R
+                plan_product4_pm(c, a.plan.words, a.plan.layers, a.plan.layer_begin, a.plan.layer_end, r);
+#pragma unroll
+                for (int h = 0; h < 4; ++h) r[h] = to_mont(pm_canon(r[h], c[h].p), c[h]);
             } else {
                 r[0] = start_residue_one<SETUP>(a, c[0], i0);
 #pragma unroll

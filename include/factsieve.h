@@ -253,7 +253,8 @@ int fs_reset_stats(fs_ctx *ctx);
  * steps, 9 generic Montgomery steps, 10 half-offset lazy 96-bit steps,
  * 11 32-bit half-offset steps, 12 shifted-window half-offset 64-bit steps,
  * 13 half-offset canonical 96-bit steps, 14 half-offset 64-bit steps with
- * the quotient on the FP32 pipe.  iters in [1, 2^24]. */
+ * the quotient on the FP32 pipe, 15 folding products modulo 2^63 + d.
+ * iters in [1, 2^24]. */
 int fs_bench_int_pipe(fs_ctx *ctx, uint32_t kind, uint32_t iters, double *ops_per_sec, double *ms);
 
 /* The residue step a segment p in [plo, phi) with multipliers up to kmax
@@ -264,6 +265,13 @@ int fs_bench_int_pipe(fs_ctx *ctx, uint32_t kind, uint32_t iters, double *ops_pe
  * beyond the forms' limits: generic Montgomery).
  * No counterpart in the reference, whose one step is the Montgomery product. */
 int fs_walk_step(uint64_t plo, uint64_t phi, uint32_t kmax);
+
+/* The setup product a segment p in [plo, phi) uses with the default
+ * four-candidate kernels and a 96-bit walk: 1 when every p is 2^63 + d with
+ * 0 < d < 2^30 (a b mod p folded with 2^64 = -2d, no Montgomery reduction),
+ * else 0 (Montgomery products).  The starting residue is the same either way.
+ * No counterpart in the reference, whose setup uses Montgomery products. */
+int fs_setup_form(uint64_t plo, uint64_t phi);
 
 /* ---- host-side pieces (no GPU needed) -------------------------------------- */
 /* Reference-format power table for n! (cl_sieve.cpp:773-838). */

@@ -294,6 +294,9 @@ def test_four_candidate_kernel_reference_selftests(ctx, variant, case):
     (10**15 + 1, 10**15 + 300_001, 100_000, 100_701),               # half-offset 96-bit walk
     (10**12 + 7, 10**12 + 300_007, 100_000, 100_701),               # lazy 64-bit, odd n-range (tail steps)
     ((1 << 33) - 150_000, (1 << 33) + 150_000, 2000, 2900),         # generic / lazy boundary
+    ((1 << 63) + (1 << 30) - 300_001, (1 << 63) + (1 << 30) - 1, 100_000, 100_301),  # folded setup, d near 2^30
+    ((1 << 63) + (1 << 30) - 150_000, (1 << 63) + (1 << 30) + 150_000, 20_000, 20_301),  # folded / Montgomery mix
+    ((1 << 63) + 1, (1 << 63) + 50_001, 1_000_000, 1_000_100),      # folded setup of 1e6! (35,800 products)
 ])
 def test_four_candidate_kernel_matches_oracle(ctx, orc, variant, lo, hi, nmin, nmax):
     want = orc.run(lo, hi, nmin, nmax)

@@ -167,6 +167,19 @@ def test_walk_step_selection_boundaries(fslib):
     assert ws(5, 5, 100) == ANY and ws(10**12, 10**12 + 5, 0) == ANY        # empty ranges
 
 
+def test_setup_form_boundaries(fslib):
+    """The setup folds its products modulo 2^63 + d exactly when every p of the
+    segment is 2^63 + d with d < 2^30 (fs_setup_form)."""
+    sf = fslib.setup_form
+    assert sf(1 << 63, (1 << 63) + 10**9) == 1                             # config 3 (2^63 is even: d >= 1)
+    assert sf(1 << 63, (1 << 63) + 10**8) == 1
+    assert sf((1 << 63) + (1 << 30) - 1000, (1 << 63) + (1 << 30)) == 1    # d up to 2^30 - 1
+    assert sf((1 << 63) + (1 << 30) - 1000, (1 << 63) + (1 << 30) + 1) == 0
+    assert sf((1 << 63) - 1000, (1 << 63) + 1000) == 0                     # straddles 2^63
+    assert sf(10**12, 10**12 + 10**9) == 0
+    assert sf((1 << 63) + 5, (1 << 63) + 5) == 0                           # empty
+
+
 def test_c_caller(fslib, tmp_path):
     """The header and library serve a plain C program (gcc, no C++ or Python in between)."""
     import shutil
