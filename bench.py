@@ -62,7 +62,7 @@ IMAD_PER_PRODUCT = 20   # reference m_mul on 32-bit limbs (8 mul_wide + 4 + 8)
 NCU_CAPTURE = {
     # config 2: a 1e8-wide capture (29,108,480 B) scaled by 10 to the whole-range launch the bench times
     "config2": {"traffic": 291_084_800, "imad_pipe_busy": 0.778, "source": "profiles/sieve_kernel_config2.md"},
-    "config3": {"traffic": 18_725_632, "imad_pipe_busy": 0.862, "source": "profiles/sieve_kernel_config3.md"},
+    "config3": {"traffic": 18_765_568, "imad_pipe_busy": 0.836, "source": "profiles/sieve_kernel_config3.md"},
 }
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 
