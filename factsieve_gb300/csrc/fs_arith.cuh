@@ -550,8 +550,8 @@ __device__ __forceinline__ u32 half_walk8x2(u32& al, u32& ah, u32& bl, u32& bh, 
 // pipe, which bounds the walk.  This step takes the quotient estimate on the
 // FP32 pipe instead and keeps four.  Let s = bitlen(f) - 4 for a floor
 // f <= p with s >= 35, z = floor(t / 2^s) and Mf = 2^s/p rounded down to
-// 24 bits.  The estimate floor(z Mf) comes from three exact float
-// instructions:
+// 24 bits.  The estimate floor(z Mf) comes from three exact instructions,
+// one integer shift and two float operations:
 //   1. A funnel shift of t's high word, with 2^(s-35) shifted in above it,
 //      gives the bit pattern of the float F = 2^-63 + z 2^-86.  Its exponent
 //      field is 64 and its mantissa is z, which needs z < 2^23.
@@ -565,8 +565,8 @@ __device__ __forceinline__ u32 half_walk8x2(u32& al, u32& ah, u32& bl, u32& bh, 
 // and the exact test is r in {x, x + 1}, as in the half-offset lazy step.
 // Validity over a launch (checked by the host, walk_for_range), with f the
 // thread's least candidate: p >= 2^38, p k_max <= 2^62, 19 k_max <= 2^23,
-// and 19 p_max k_max < 2^(bitlen(p_min) + 23), which keeps z < 2^23.  The two float instructions
-// have no .ftz, so subnormals are kept.
+// and 19 p_max k_max < 2^(bitlen(p_min) + 23), which keeps z < 2^23.  The
+// two float instructions have no .ftz, so subnormals are kept.
 struct HalfF {
     u64 p, x;
     u32 np0, np1;             // 2^64 - p
