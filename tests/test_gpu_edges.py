@@ -113,14 +113,14 @@ def test_plan_check_flags_a_corrupted_plan(ctx, what):
 
 
 def test_ceiling_kernels_report_rates(ctx):
-    """The roofline's ceiling microkernels (fs_bench_int_pipe kinds 0-14) run and
+    """The roofline's ceiling microkernels (fs_bench_int_pipe kinds 0-15) run and
     report plausible rates; an unknown kind is refused."""
     import factsieve_gb300 as fs
-    rates = {k: ctx.bench_int_pipe(k, 200)[0] for k in range(15)}
+    rates = {k: ctx.bench_int_pipe(k, 200)[0] for k in range(16)}
     assert all(v > 0 for v in rates.values()), rates
     assert rates[0] > rates[4]             # an IMAD issues faster than a Montgomery product completes
     with pytest.raises(fs.FSError):
-        ctx.bench_int_pipe(15, 200)
+        ctx.bench_int_pipe(16, 200)
     with pytest.raises(fs.FSError):
         ctx.bench_int_pipe(5, 0)
 
