@@ -127,7 +127,11 @@ def roofline(ctx, fs, wl, ncand, st, step_ms, clocks=None, seg=None):
     mm_ceil, _ = ctx.bench_int_pipe(4, 4000)
     imad_ops, _ = ctx.bench_int_pipe(0, 20000)
     folded = bool(fs.setup_form(pmin, min(pmin + seg, pmax))) and step in (3, 8)
-    plan_ceil = ctx.bench_int_pipe(15, 4000)[0] if folded else mm_ceil
+    # the folding product's own ceiling is below Montgomery's at full occupancy
+    # (it wins inside the fused kernel, at 2 blocks per SM): the peak takes the
+    # faster of the two, so it never rests on the slower form
+    fold_ceil = ctx.bench_int_pipe(15, 4000)[0] if folded else None
+    plan_ceil = max(fold_ceil, mm_ceil) if folded else mm_ceil
     plan_products, mont_products = setup_products(fs, nmin, folded)
     smp = plan_products + mont_products
     sieve_s = st["sieve_ms"] * 1e-3
@@ -161,7 +165,8 @@ def roofline(ctx, fs, wl, ncand, st, step_ms, clocks=None, seg=None):
         "share_of_step": st["sieve_ms"] / step_ms if step_ms else None,
         "walk_step": step_name,
         "ceilings": {"walk_steps_per_s": walk_ceil, "montgomery_products_per_s": mm_ceil,
-                     "plan_products_per_s": plan_ceil, "imad_lane_ops_per_s": imad_ops},
+                     "folding_products_per_s": fold_ceil, "plan_products_per_s": plan_ceil,
+                     "imad_lane_ops_per_s": imad_ops},
         "setup_products_per_candidate": smp,
         "setup_product": "folding modulo 2^63 + d" if folded else "Montgomery",
         "peak_source": "measured on this GPU: the walk step's PTX block and mont_mul, register-resident at full "
