@@ -376,3 +376,50 @@ def test_random_ranges_match_oracle(ctx, orc, lo, hi, nmin, nmax):
     ctx.synchronize()
     cs = _counters(ctr)
     assert (int(cs["raw_sum"]), int(cs["flags"]), int(cs["nhits"])) == (want["raw_sum"], 0, want["nhits"])
+
+
+def _regime_cases(seed):
+    """Seeded ranges inside the two forms that need launch-wide proofs: the
+    float-quotient walk (p >= 2^38, k_max <= 441,505 and its z bound) and the
+    folded setup (p in (2^63, 2^63 + 2^30)), with bounds chosen near their
+    edges as often as inside."""
+    import random
+    import factsieve_gb300 as fs
+    rng = random.Random(seed)
+    out = []
+    while len(out) < 48:
+        bits = rng.randrange(38, 60)
+        lo = rng.randrange(1 << bits, 1 << (bits + 1))
+        kmax = rng.choice([rng.randrange(300, 441_506), rng.randrange(430_000, 441_506)])
+        lo, w = rng.choice([(lo, rng.randrange(2000, 40_000)), ((1 << bits) - 20_000, 40_000)])
+        nmin = max(34, kmax - rng.randrange(1, 1500))
+        if fs.walk_step(lo, lo + w, kmax) == 9:
+            out.append((lo, lo + w, nmin, kmax))
+    while len(out) < 80:
+        d = rng.choice([rng.randrange(0, (1 << 30) - 50_000), (1 << 30) - 40_001])
+        lo, w = (1 << 63) + d, rng.randrange(2000, 40_000)
+        nmin = rng.choice([rng.randrange(34, 2000), rng.randrange(2000, 300_000)])
+        if fs.setup_form(lo, lo + w):
+            out.append((lo, lo + w, nmin, nmin + rng.randrange(1, 800)))
+    return out
+
+
+@pytest.mark.parametrize("variant", [5, 3])
+def test_random_float_quotient_and_folded_setup_ranges(ctx, orc, variant):
+    """Seeded random ranges of the float-quotient walk step and of the folded
+    setup products, searched with ragged segment widths by both kernel builds:
+    every one equals the oracle bit for bit."""
+    import random
+    rng = random.Random(5 + variant)
+    bad = []
+    try:
+        ctx.set_tuning(sieve_variant=variant)
+        for lo, hi, nmin, nmax in _regime_cases(20261204):
+            want = orc.run(lo, hi, nmin, nmax)
+            r = ctx.sieve(lo, hi, nmin, nmax, seg_width=rng.choice([7_777, 50_000, 10**6]))
+            if (r.primecount, r.raw_sum, r.checksum, r.factorcount) != \
+                    (want["primecount"], want["raw_sum"], want["checksum"], want["factorcount"]):
+                bad.append((lo, hi, nmin, nmax))
+    finally:
+        ctx.set_tuning()
+    assert not bad, bad
