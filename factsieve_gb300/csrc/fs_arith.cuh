@@ -227,15 +227,22 @@ __device__ __forceinline__ u64 lazy_canon(u64 r, const Lazy64& L) { return r >= 
     "setp.eq.or.u32 P, " RL ", " C1 ", P;\n\t"         \
     "setp.eq.or.u32 P, " RL ", " C2 ", P;\n\t"         \
     "setp.eq.or.u32 P, " RL ", " C3 ", P;\n\t"
+// r' = t + q (2^64 - p) is formed by a mad.lo.cc / madc.hi carry pair and
+// one mad.lo rather than by a mad.wide with a 64-bit addend: on GB300 the
+// latter costs two more integer ALU instructions per step (ncu), and these
+// walk blocks are bound by instruction issue as much as by the multiply pipe
+// (lazy 64-bit ceiling +17 %, half-offset +6 %, float quotient +8 %).  The
+// blocks that keep the multiply pipe above 90 % busy (the half-offset 96-bit
+// and canonical 96-bit-in-half-offset steps) keep the mad.wide form, where
+// the extra lo/hi pipe cycles cost more than the saved ALU work.
 #define FS_LZ_MUL(RL, RH, NP0, NP1, MM, T, R, TL, TH, Q)          \
     "mul.wide.u32 " T ", " RL ", kk;\n\t"                          \
     "mov.b64 {" TL ", " TH "}, " T ";\n\t"                         \
     "mad.lo.u32 " TH ", " RH ", kk, " TH ";\n\t"                   \
     "mul.hi.u32 " Q ", " TH ", " MM ";\n\t"                        \
-    "mov.b64 " T ", {" TL ", " TH "};\n\t"                         \
-    "mad.wide.u32 " R ", " Q ", " NP0 ", " T ";\n\t"               \
-    "mov.b64 {" RL ", " RH "}, " R ";\n\t"                         \
-    "mad.lo.u32 " RH ", " Q ", " NP1 ", " RH ";\n\t"
+    "mad.lo.cc.u32 " RL ", " Q ", " NP0 ", " TL ";\n\t"          \
+    "madc.hi.u32 " TH ", " Q ", " NP0 ", " TH ";\n\t"            \
+    "mad.lo.u32 " RH ", " Q ", " NP1 ", " TH ";\n\t"
 #define FS_LZ_STEP2(J)                                              \
     "add.u32 kk, %5, " #J ";\n\t"                                   \
     FS_LZ_TEST("%0", "%9", "%10", "%11", "%12")                     \
@@ -372,15 +379,13 @@ __device__ __forceinline__ u64 canon96_step(u64 r, u32 k, const Canon96& C) {
 #define FS_L96_MUL(RL, RH, NP0, NP1, MM, SH, T, U, R, CC, T0, C, T1, T2, Z, Q)  \
     "mul.wide.u32 " T ", " RL ", kk;\n\t"                                        \
     "mov.b64 {" T0 ", " C "}, " T ";\n\t"                                        \
-    "mov.b64 " CC ", {" C ", zr};\n\t"                                           \
-    "mad.wide.u32 " U ", " RH ", kk, " CC ";\n\t"                                \
-    "mov.b64 {" T1 ", " T2 "}, " U ";\n\t"                                       \
+    "mad.lo.cc.u32 " T1 ", " RH ", kk, " C ";\n\t"                               \
+    "madc.hi.u32 " T2 ", " RH ", kk, zr;\n\t"                                       \
     "shf.r.clamp.b32 " Z ", " T1 ", " T2 ", " SH ";\n\t"                         \
     "mul.hi.u32 " Q ", " Z ", " MM ";\n\t"                                       \
-    "mov.b64 " T ", {" T0 ", " T1 "};\n\t"                                       \
-    "mad.wide.u32 " R ", " Q ", " NP0 ", " T ";\n\t"                             \
-    "mov.b64 {" RL ", " RH "}, " R ";\n\t"                                       \
-    "mad.lo.u32 " RH ", " Q ", " NP1 ", " RH ";\n\t"
+    "mad.lo.cc.u32 " RL ", " Q ", " NP0 ", " T0 ";\n\t"                          \
+    "madc.hi.u32 " T1 ", " Q ", " NP0 ", " T1 ";\n\t"                            \
+    "mad.lo.u32 " RH ", " Q ", " NP1 ", " T1 ";\n\t"
 #define FS_L96_STEP2(J)                                                                        \
     "add.u32 kk, %5, " #J ";\n\t"                                                              \
     FS_LZ_TEST("%0", "%10", "%11", "%12", "%13")                                               \
@@ -415,16 +420,14 @@ __device__ __forceinline__ u32 lazy96_walk8x2(u32& al, u32& ah, u32& bl, u32& bh
 #define FS_C96_MUL(RL, RH, P0, P1, MM, SH, PP, T, U, A, B, CC, R64, T0, C, T1, T2, Z, Q, X0, X1, Y1, Y2, W2, G) \
     "mul.wide.u32 " T ", " RL ", kk;\n\t"                                        \
     "mov.b64 {" T0 ", " C "}, " T ";\n\t"                                        \
-    "mov.b64 " CC ", {" C ", zr};\n\t"                                           \
-    "mad.wide.u32 " U ", " RH ", kk, " CC ";\n\t"                                \
-    "mov.b64 {" T1 ", " T2 "}, " U ";\n\t"                                       \
+    "mad.lo.cc.u32 " T1 ", " RH ", kk, " C ";\n\t"                               \
+    "madc.hi.u32 " T2 ", " RH ", kk, zr;\n\t"                                       \
     "shf.r.clamp.b32 " Z ", " T1 ", " T2 ", " SH ";\n\t"                         \
     "mul.hi.u32 " Q ", " Z ", " MM ";\n\t"                                       \
     "mul.wide.u32 " A ", " Q ", " P0 ";\n\t"                                     \
     "mov.b64 {" X0 ", " X1 "}, " A ";\n\t"                                       \
-    "mov.b64 " CC ", {" X1 ", zr};\n\t"                                          \
-    "mad.wide.u32 " B ", " Q ", " P1 ", " CC ";\n\t"                             \
-    "mov.b64 {" Y1 ", " Y2 "}, " B ";\n\t"                                       \
+    "mad.lo.cc.u32 " Y1 ", " Q ", " P1 ", " X1 ";\n\t"                           \
+    "madc.hi.u32 " Y2 ", " Q ", " P1 ", zr;\n\t"                                       \
     "sub.cc.u32 " RL ", " T0 ", " X0 ";\n\t"                                     \
     "subc.cc.u32 " RH ", " T1 ", " Y1 ";\n\t"                                    \
     "subc.u32 " W2 ", " T2 ", " Y2 ";\n\t"                                       \
@@ -629,10 +632,9 @@ __device__ __forceinline__ u64 halff_canon(u64 r, const HalfF& H) { return r >= 
     "sub.rn.f32 " F ", " F ", 0f20000000;\n\t"                           \
     "fma.rm.f32 " F ", " F ", " MF ", 0f00000000;\n\t"                   \
     "mov.b32 " Q ", " F ";\n\t"                                          \
-    "mov.b64 " T ", {" TL ", " TH "};\n\t"                               \
-    "mad.wide.u32 " R ", " Q ", " NP0 ", " T ";\n\t"                     \
-    "mov.b64 {" RL ", " RH "}, " R ";\n\t"                               \
-    "mad.lo.u32 " RH ", " Q ", " NP1 ", " RH ";\n\t"
+    "mad.lo.cc.u32 " RL ", " Q ", " NP0 ", " TL ";\n\t"                  \
+    "madc.hi.u32 " TH ", " Q ", " NP0 ", " TH ";\n\t"                    \
+    "mad.lo.u32 " RH ", " Q ", " NP1 ", " TH ";\n\t"
 // The multipliers k1 .. k1 + 7 come in as operands %20-%27: computed outside
 // the asm, they are shared by the blocks of a thread's two pairs.
 #define FS_HFF_STEP2(KK)                                                                             \
@@ -705,12 +707,27 @@ __device__ __forceinline__ u64 half96_step(u64 r, u32 k, const Half96& H) {
 }
 __device__ __forceinline__ u64 half96_canon(u64 r, const Half96& H) { return r >= H.p ? r - H.p : r; }
 
+// The lazy 96-bit multiply with mad.wide and 64-bit addends: for the
+// half-offset 96-bit step this form measures 2 % faster than the carry-pair
+// form that FS_L96_MUL uses.
+#define FS_H96_MUL(RL, RH, NP0, NP1, MM, SH, T, U, R, CC, T0, C, T1, T2, Z, Q)  \
+    "mul.wide.u32 " T ", " RL ", kk;\n\t"                                        \
+    "mov.b64 {" T0 ", " C "}, " T ";\n\t"                                        \
+    "mov.b64 " CC ", {" C ", zr};\n\t"                                           \
+    "mad.wide.u32 " U ", " RH ", kk, " CC ";\n\t"                                \
+    "mov.b64 {" T1 ", " T2 "}, " U ";\n\t"                                       \
+    "shf.r.clamp.b32 " Z ", " T1 ", " T2 ", " SH ";\n\t"                         \
+    "mul.hi.u32 " Q ", " Z ", " MM ";\n\t"                                       \
+    "mov.b64 " T ", {" T0 ", " T1 "};\n\t"                                       \
+    "mad.wide.u32 " R ", " Q ", " NP0 ", " T ";\n\t"                             \
+    "mov.b64 {" RL ", " RH "}, " R ";\n\t"                                       \
+    "mad.lo.u32 " RH ", " Q ", " NP1 ", " RH ";\n\t"
 #define FS_H96_STEP2(J)                                                                        \
     "add.u32 kk, %5, " #J ";\n\t"                                                              \
     FS_HF_TEST("%0", "%10", "%11")                                                             \
     FS_HF_TEST("%2", "%16", "%17")                                                             \
-    FS_L96_MUL("%0", "%1", "%6", "%7", "%8", "%9", "TA", "UA", "RA", "CA", "a0", "ac", "a1", "a2", "az", "aq") \
-    FS_L96_MUL("%2", "%3", "%12", "%13", "%14", "%15", "TB", "UB", "RB", "CB", "b0", "bc", "b1", "b2", "bz", "bq")
+    FS_H96_MUL("%0", "%1", "%6", "%7", "%8", "%9", "TA", "UA", "RA", "CA", "a0", "ac", "a1", "a2", "az", "aq") \
+    FS_H96_MUL("%2", "%3", "%12", "%13", "%14", "%15", "TB", "UB", "RB", "CB", "b0", "bc", "b1", "b2", "bz", "bq")
 
 __device__ __forceinline__ u32 half96_walk8x2(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const Half96& A,
                                               const Half96& B) {
@@ -843,10 +860,9 @@ __device__ __forceinline__ u64 halfmid_step(u64 r, u32 k, const Half96& H) {
     "mad.lo.u32 " TH ", " RH ", kk, " TH ";\n\t"                   \
     "shf.r.clamp.b32 " Z ", " TL ", " TH ", " SH ";\n\t"           \
     "mul.hi.u32 " Q ", " Z ", " MM ";\n\t"                         \
-    "mov.b64 " T ", {" TL ", " TH "};\n\t"                         \
-    "mad.wide.u32 " R ", " Q ", " NP0 ", " T ";\n\t"               \
-    "mov.b64 {" RL ", " RH "}, " R ";\n\t"                         \
-    "mad.lo.u32 " RH ", " Q ", " NP1 ", " RH ";\n\t"
+    "mad.lo.cc.u32 " RL ", " Q ", " NP0 ", " TL ";\n\t"          \
+    "madc.hi.u32 " TH ", " Q ", " NP0 ", " TH ";\n\t"            \
+    "mad.lo.u32 " RH ", " Q ", " NP1 ", " TH ";\n\t"
 #define FS_HM_STEP2(J)                                                                   \
     "add.u32 kk, %5, " #J ";\n\t"                                                        \
     FS_HF_TEST("%0", "%10", "%11")                                                       \
