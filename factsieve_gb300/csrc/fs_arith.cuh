@@ -233,8 +233,8 @@ __device__ __forceinline__ u64 lazy_canon(u64 r, const Lazy64& L) { return r >= 
 // walk blocks are bound by instruction issue as much as by the multiply pipe
 // (lazy 64-bit ceiling +17 %, half-offset +6 %, float quotient +8 %).  The
 // blocks that keep the multiply pipe above 90 % busy (the half-offset 96-bit
-// and canonical 96-bit-in-half-offset steps) keep the mad.wide form, where
-// the extra lo/hi pipe cycles cost more than the saved ALU work.
+// step and the half-offset canonical 96-bit step) keep the mad.wide form,
+// where the extra lo/hi pipe cycles cost more than the saved ALU work.
 #define FS_LZ_MUL(RL, RH, NP0, NP1, MM, T, R, TL, TH, Q)          \
     "mul.wide.u32 " T ", " RL ", kk;\n\t"                          \
     "mov.b64 {" TL ", " TH "}, " T ";\n\t"                         \
@@ -549,9 +549,10 @@ __device__ __forceinline__ u32 half_walk8x2(u32& al, u32& ah, u32& bl, u32& bh, 
 
 // ------------- iterate: half-offset 64-bit steps, quotient on the FP32 pipe --
 //
-// The half-offset lazy 64-bit step runs five products on the integer multiply
-// pipe, which bounds the walk.  This step takes the quotient estimate on the
-// FP32 pipe instead and keeps four.  Let s = bitlen(f) - 4 for a floor
+// The half-offset lazy 64-bit step takes its quotient estimate with an
+// IMAD.HI on the integer multiply pipe, which bounds the walk.  This step
+// takes it on the FP32 pipe instead and keeps the multiplies that form
+// t = r k and r' = t + q (2^64 - p).  Let s = bitlen(f) - 4 for a floor
 // f <= p with s >= 35, z = floor(t / 2^s) and Mf = 2^s/p rounded down to
 // 24 bits.  The estimate floor(z Mf) comes from three exact instructions,
 // one integer shift and two float operations:
