@@ -203,3 +203,98 @@ def test_c_caller(fslib, tmp_path):
     assert int(got["capacity"]) == fslib.candidate_capacity(10**12, 10**12 + 10**8)
     assert got["walk_step"] == "9 6"
     assert got["strerror"].strip() == fslib.lib().fs_strerror(fslib.FS_E_OVERFLOW).decode()
+
+
+def _f32(bits):
+    import struct
+    from fractions import Fraction
+    return Fraction(struct.unpack("<f", struct.pack("<I", bits & 0xFFFFFFFF))[0])
+
+
+def _halff_step(r, k, p, f):
+    """Word-level restatement of halff_step (fs_arith.cuh) with exact rationals:
+    funnel shift into the float 2^-63 + z 2^-86, exact subtraction, fma rounding
+    down onto the subnormal grid."""
+    from fractions import Fraction
+    bl, s = p.bit_length(), f.bit_length() - 4
+    e = bl + 23
+    m = (1 << e) // p
+    mf = _f32(((s - bl + 63) << 23) + m)
+    assert mf == Fraction(m, 1 << (e - s + 63))
+    sh, hc = s - 32, 1 << (s - 35)
+    t = r * k
+    assert t < 1 << 64
+    th = t >> 32
+    z = th >> sh
+    assert z < 1 << 23
+    fbits = (z | (hc << (32 - sh))) & 0xFFFFFFFF
+    assert _f32(fbits) == Fraction(1, 1 << 63) + Fraction(z, 1 << 86)
+    prod = (_f32(fbits) - Fraction(1, 1 << 63)) * mf
+    assert prod < Fraction(1, 1 << 126)
+    q = int(prod * (1 << 149))
+    return (t + q * ((1 << 64) - p)) % (1 << 64)
+
+
+def test_float_quotient_window_holds_where_the_host_selects_it(fslib):
+    """Wherever fs_walk_step picks the float-quotient step, the step is exact and
+    keeps r below (19/16) p < x + p, the bound the two-compare hit test needs.
+    Checked for the least and largest p of each range, with the thread floor at
+    the range's low end, over the last multipliers up to k_max."""
+    import random
+    rng = random.Random(3)
+    n = 0
+    while n < 40:
+        bits = rng.randrange(38, 61)
+        lo = rng.randrange(1 << bits, 1 << (bits + 1))
+        w = rng.choice([1000, 10**6, 1 << (bits - 2)])
+        kmax = rng.choice([rng.randrange(2, 441_506), 441_505])
+        if fslib.walk_step(lo, lo + w, kmax) != 9:
+            continue
+        n += 1
+        for p in (lo | 1, (lo + w - 1) | 1):
+            if p >= lo + w:
+                p -= 2
+            r = p - 1
+            for k in range(max(1, kmax - 150), kmax + 1):
+                r2 = _halff_step(r, k, p, lo)
+                assert r2 % p == (r * k) % p
+                assert 16 * r2 < 19 * p
+                r = r2
+
+
+def _pm_mul(a, b, p):
+    """Word-level restatement of pm_mul (fs_arith.cuh): fold 2^64 = -2d modulo
+    p = 2^63 + d twice, add p - 2d on a carry out."""
+    M = (1 << 64) - 1
+    e = 2 * (p - (1 << 63))
+    x = a * b
+    x0, x1 = x & M, x >> 64
+    w = e * x1
+    w0, w1 = w & M, w >> 64
+    assert w1 < e
+    u, borrow = (x0 - w0) & M, int(x0 < w0)
+    v = e * (w1 + borrow)
+    assert v < 1 << 62
+    y = u + v
+    if y >> 64:
+        y = (y & M) + (p - e)
+        assert y < 1 << 64
+    return y
+
+
+def test_folded_product_is_exact_where_the_host_selects_it(fslib):
+    """Wherever fs_setup_form selects the folding product, it is congruent to a b
+    for any 64-bit inputs and stays below 2^64, over chains as the setup runs them."""
+    import random
+    rng = random.Random(4)
+    for _ in range(30):
+        d = rng.choice([1, rng.randrange(1, 1 << 30), (1 << 30) - 1]) | 1
+        p = (1 << 63) + d
+        assert fslib.setup_form(p, p + 1) == 1
+        x, ex = 1, 1
+        for _ in range(200):
+            w = rng.choice([rng.randrange(1 << 64), (1 << 64) - 1, 2, p, p - 1])
+            x = _pm_mul(x, w, p)
+            ex = ex * w % p
+            assert x < 1 << 64 and x % p == ex
+        assert _pm_mul((1 << 64) - 1, (1 << 64) - 1, p) % p == ((1 << 64) - 1) ** 2 % p
