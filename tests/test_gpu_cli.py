@@ -123,7 +123,7 @@ def test_cli_top_of_the_p_range(fslib, orc, tmp_path):
 
 
 @pytest.mark.parametrize("name,argv", [
-    ("config2", ["-n", "1e5", "-N", "2e5", "-p", "1e12", "-P", "1001e9"]),          # the survey's own spelling
+    ("config2", ["-n", "1e5", "-N", "2e5", "-p", "1e12", "-P", "1001e9"]),          # suffix spellings of 1e12 + 1e9
     ("config3", ["-n", "1e6", "-N", "101e4", "-p", "9223372036854775808", "-P", "9223372037854775808"]),
 ])
 def test_cli_full_config_matches_oracle_fixture(fslib, tmp_path, name, argv):
