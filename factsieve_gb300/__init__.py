@@ -20,7 +20,7 @@ import numpy as np
 
 __all__ = ["lib", "Context", "Tuning", "SieveResult", "FSError", "LibraryMissing", "sieve",
            "power_table", "setup_plan", "is_prime", "verify_factor", "postprocess",
-           "find_wheel_offset", "candidate_capacity", "FACTOR_DTYPE", "COUNTERS_DTYPE"]
+           "find_wheel_offset", "candidate_capacity", "walk_state_words", "FACTOR_DTYPE", "COUNTERS_DTYPE"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libfactsieve.so")
@@ -228,6 +228,12 @@ def verify_factor(p: int, n: int, c: int) -> bool:
 
 def candidate_capacity(low: int, high: int) -> int:
     return lib().fs_candidate_capacity(low, high)
+
+
+def walk_state_words(cap: int) -> int:
+    """u64 words of a stage-level residue buffer for cap candidates
+    (FS_WALK_STATE_WORDS): cap residues, then cap uint32 walked-n tags."""
+    return cap + (cap + 1) // 2
 
 
 def postprocess(hits: np.ndarray, threads: int = 2):

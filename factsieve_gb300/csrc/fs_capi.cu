@@ -290,7 +290,7 @@ int run_sieve(fs_ctx* c, const u64* d_cand, uint32_t cap, fs::Counters* d_ctr, u
     const uint32_t maxs = c->tuning.max_steps_per_launch;
     const bool split = maxs && span > maxs;
     if (split) {
-        if ((rc = grow(c, &c->d_residue, &c->residue_cap, (uint64_t)cap + 1))) return rc;
+        if ((rc = grow(c, &c->d_residue, &c->residue_cap, FS_WALK_STATE_WORDS(cap)))) return rc;
     }
     fs::SieveArgs a = base_args(pl);
     a.cand = d_cand;
@@ -321,9 +321,10 @@ int run_sieve(fs_ctx* c, const u64* d_cand, uint32_t cap, fs::Counters* d_ctr, u
         const bool fin = (e == nend);
         a.nstart = s;
         a.nend = e;
+        // split launches carry residues and the n each stands at (its tag) from one launch to the next
         a.residue = split ? c->d_residue : nullptr;
+        a.walked = split ? (u32*)(c->d_residue + cap) : nullptr;
         a.count_candidates = (fin && count) ? 1u : 0u;
-        a.store_final = 0;
         std::pair<cudaEvent_t, cudaEvent_t> ev;
         if ((rc = ev_begin(c, &ev))) return rc;
         const int kv = kernel_variant(variant(c), walk);
@@ -662,6 +663,7 @@ int fs_setup(fs_ctx* c, const uint64_t* d_cand, uint32_t cap, fs_counters* d_ctr
     a.cap = cap;
     a.ctr = (fs::Counters*)d_ctr;
     a.residue = (u64*)d_residue;
+    a.walked = (u32*)((u64*)d_residue + cap);
     a.nstart = a.nend = nstart;
     int mode = fs::SETUP_PLAN;
     if (chunks > 1) {
@@ -686,6 +688,7 @@ int fs_iterate(fs_ctx* c, const uint64_t* d_cand, uint32_t cap, fs_counters* d_c
     a.cap = cap;
     a.ctr = (fs::Counters*)d_ctr;
     a.residue = (u64*)d_residue;
+    a.walked = (u32*)((u64*)d_residue + cap);
     a.hits = (fs::Factor*)d_hits;
     a.hitcap = hitcap;
     const uint32_t maxs = c->tuning.max_steps_per_launch;
@@ -711,10 +714,10 @@ int fs_check(fs_ctx* c, const uint64_t* d_cand, uint32_t cap, fs_counters* d_ctr
     a.cap = cap;
     a.ctr = (fs::Counters*)d_ctr;
     a.residue = (u64*)d_residue;
+    a.walked = (u32*)((u64*)d_residue + cap);
     a.nstart = a.nend = nmax;
     a.nmax = nmax;
     a.count_candidates = 1;
-    a.store_final = 0;
     CK(c, fs::launch_sieve(a, fs::SETUP_LOAD, true, sieve_grid(c, any_variant(c)), c->stream, any_variant(c), fs::WALK_ANY));
     return FS_OK;
 }

@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(kGenWarps * 32) gen_kernel(GenArgs a) {
     const u64 stride = (u64)gridDim.x * blockDim.x;
     for (u64 wb = (u64)blockIdx.x * blockDim.x; wb < a.nwords; wb += stride) {
         const u64 w = wb + threadIdx.x;
-        const u32 w32 = (u32)w;          // the host keeps nwords below 2^32
+        const u32 w32 = (u32)w;          // the host keeps nwords below 2^31
         u32 sv = 0;
         if (w < a.nwords) {
             u32 comp = 0;
@@ -77,18 +77,22 @@ __global__ void __launch_bounds__(kGenWarps * 32) gen_kernel(GenArgs a) {
         }
         const u32 total = __shfl_sync(0xffffffffu, incl, 31);
         u32 off = incl - cnt;
+        // Odd index relative to the block's first word wb: below 256 * 32, so
+        // it fits a u32 for any segment width (an index relative to o0 would
+        // wrap once w reaches 2^27).
         while (sv) {
             int i = __ffs(sv) - 1;
             sv &= sv - 1;
-            queue[warp][off++] = w32 * 32u + (u32)i;   // odd index relative to o0
+            queue[warp][off++] = (u32)threadIdx.x * 32u + (u32)i;
         }
         __syncwarp();
+        const u64 block_o = a.o0 + 64 * wb;
         for (u32 jb = 0; jb < total; jb += 32) {
             const u32 j = jb + lane;
             bool pass = false;
             u64 n = 0;
             if (j < total) {
-                n = a.o0 + 2 * (u64)queue[warp][j];
+                n = block_o + 2 * (u64)queue[warp][j];
                 pass = sprp2(n);
             }
             const u32 bal = __ballot_sync(0xffffffffu, pass);

@@ -36,6 +36,8 @@ struct SieveArgs {
     const u32* ncand;     // device count (read by the kernel)
     u32 cap;              // capacity of cand[] / residue[]
     u64* residue;         // starting residues (SETUP_LOAD), updated residues (non-final)
+    u32* walked;          // per candidate, the n its residue stands at (read with SETUP_LOAD, written by
+                          // non-final launches); nullptr: no earlier launch, residues start at nstart
     u64* partials;        // SETUP_PARTIALS: nchunks x cap partial products
     u32 nchunks;
     const PlanChunkDev* chunks;
@@ -43,7 +45,6 @@ struct SieveArgs {
     u32 nstart, nend;     // walk n over [nstart, nend)
     u32 nmax;             // final n (s7 = nmax * R) on the final chunk
     u32 count_candidates; // final chunk adds ncand to the candidate total
-    u32 store_final;      // final chunk also writes the end residues to residue[]
     Factor* hits;
     u32 hitcap;
     Counters* ctr;
@@ -68,7 +69,7 @@ struct TableCheckArgs {
 struct BatchJob {
     const u64* cand;
     u32 cap;
-    u32 nstart, nend;            // walk [nstart, nend); s7 = nend * R
+    u32 nstart, nend;            // walk [nstart, nend); the walk must reach nend (= the job's nmax)
     u32 layer_begin, layer_end;  // its plan's layers in the shared layer table
     u32 walk;                    // WALK_* step valid for the job's whole p-range
     u64 deficit;
@@ -95,13 +96,15 @@ enum : u32 { SERVE_SETUP = 1u, SERVE_FINAL = 2u };
 struct ServeChunk {
     const u64* cand;
     u64* residue;
+    u32* walked;                 // per candidate, the n its residue stands at between rounds
     Counters* ctr;               // the job's counters (raw_sum, flags)
     const u64* words;            // the job's setup plan
     const Layer* layers;
     u64 deficit;
     u32 layer_begin, layer_end;
     u32 first, count;            // candidates [first, first + count)
-    u32 nstart, nend;            // walk [nstart, nend); final: s7 = nend * R
+    u32 nstart, nend;            // walk [nstart, nend)
+    u32 nmax;                    // the job's nmax: a final chunk's walks must have reached it
     u32 flags;                   // SERVE_SETUP: start from the plan; SERVE_FINAL: checksum, no store
     u32 tag;                     // job slot, stored in hit records
     u32 tile_end;                // inclusive prefix of tiles over the round's chunks

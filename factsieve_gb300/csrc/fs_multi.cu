@@ -63,9 +63,10 @@ __global__ void __launch_bounds__(kSieveThreads, 2) batch_sieve_kernel(BatchArgs
 #pragma unroll
             for (int h = 0; h < 4; ++h) r[h] = mont_mul(r[h], mont_pow(c[h].r2, J.deficit, c[h]), c[h].p, c[h].pinv);
             walk_quad_rt((int)J.walk, r, c, nreal, J.nstart, J.nend, o);
+            // one launch walks the job's whole n-range: its residues stand at nend = the job's nmax
 #pragma unroll
             for (int h = 0; h < 4; ++h)
-                if ((u32)h < nreal) final_check(c[h], r[h], J.nend, sum, bad);
+                if ((u32)h < nreal) final_check(c[h], r[h], J.nend, J.nend, sum, bad);
         }
 #pragma unroll
         for (int d = 16; d; d >>= 1) {
@@ -148,7 +149,8 @@ __global__ void __launch_bounds__(kSieveThreads, PPT == 4 ? 2 : 3) serve_round_k
                 Prime c[4];
                 const u32 nreal = load_quad(T.cand, i0, end, c);
                 u64 r[4];
-                if (T.flags & SERVE_SETUP) {
+                const bool setup = T.flags & SERVE_SETUP;
+                if (setup) {
                     plan_product4(c, T.words, T.layers, T.layer_begin, T.layer_end, r);
 #pragma unroll
                     for (int h = 0; h < 4; ++h)
@@ -159,21 +161,26 @@ __global__ void __launch_bounds__(kSieveThreads, PPT == 4 ? 2 : 3) serve_round_k
                     for (int h = 1; h < 4; ++h) r[h] = (u32)h < nreal ? T.residue[i0 + h] : r[0];
                 }
                 walk_quad_rt((int)T.walk, r, c, nreal, T.nstart, T.nend, o);
-                if (T.flags & SERVE_FINAL) {
+                const u32 steps = T.nend > T.nstart ? T.nend - T.nstart : 0;
 #pragma unroll
-                    for (int h = 0; h < 4; ++h)
-                        if ((u32)h < nreal) final_check(c[h], r[h], T.nend, sum, bad);
-                } else {
-#pragma unroll
-                    for (int h = 0; h < 4; ++h)
-                        if ((u32)h < nreal) T.residue[i0 + h] = r[h];
+                for (int h = 0; h < 4; ++h) {
+                    if ((u32)h >= nreal) break;
+                    // the n this candidate's residue stands at: its tag, advanced by the walk
+                    const u32 nw = (setup ? T.nstart : T.walked[i0 + h]) + steps;
+                    if (T.flags & SERVE_FINAL) {
+                        final_check(c[h], r[h], nw, T.nmax, sum, bad);
+                    } else {
+                        T.residue[i0 + h] = r[h];
+                        T.walked[i0 + h] = nw;
+                    }
                 }
             } else {
                 const bool real_b = i0 + 1 < end;
                 const Prime ca = make_prime(T.cand[i0]);
                 const Prime cb = real_b ? make_prime(T.cand[i0 + 1]) : ca;
                 u64 ra, rb;
-                if (T.flags & SERVE_SETUP) {
+                const bool setup = T.flags & SERVE_SETUP;
+                if (setup) {
                     plan_product2(ca, cb, T.words, T.layers, T.layer_begin, T.layer_end, ra, rb);
                     ra = mont_mul(ra, mont_pow(ca.r2, T.deficit, ca), ca.p, ca.pinv);
                     rb = mont_mul(rb, mont_pow(cb.r2, T.deficit, cb), cb.p, cb.pinv);
@@ -182,12 +189,19 @@ __global__ void __launch_bounds__(kSieveThreads, PPT == 4 ? 2 : 3) serve_round_k
                     rb = real_b ? T.residue[i0 + 1] : ra;
                 }
                 walk_pair(ra, rb, ca, cb, real_b, T.nstart, T.nend, o);
+                const u32 steps = T.nend > T.nstart ? T.nend - T.nstart : 0;
+                const u32 nwa = (setup ? T.nstart : T.walked[i0]) + steps;
+                const u32 nwb = real_b ? (setup ? T.nstart : T.walked[i0 + 1]) + steps : nwa;
                 if (T.flags & SERVE_FINAL) {
-                    final_check(ca, ra, T.nend, sum, bad);
-                    if (real_b) final_check(cb, rb, T.nend, sum, bad);
+                    final_check(ca, ra, nwa, T.nmax, sum, bad);
+                    if (real_b) final_check(cb, rb, nwb, T.nmax, sum, bad);
                 } else {
                     T.residue[i0] = ra;
-                    if (real_b) T.residue[i0 + 1] = rb;
+                    T.walked[i0] = nwa;
+                    if (real_b) {
+                        T.residue[i0 + 1] = rb;
+                        T.walked[i0 + 1] = nwb;
+                    }
                 }
             }
         }

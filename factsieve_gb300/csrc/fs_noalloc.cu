@@ -29,7 +29,8 @@ struct DeviceState {
     bool ready = false;
     u64* cand = nullptr;   // device address of g_noalloc_cand on this device
     int sm_count = 0;
-    int blocks_per_sm = 1;
+    int occ3 = 1;          // resident blocks per SM of the two-candidate build
+    int occ5 = 1;          // and of the four-candidate build
 };
 
 constexpr int kMaxDevices = 64;
@@ -46,12 +47,14 @@ int device_state(DeviceState** out) {
     if (!s.ready) {
         void* ptr = nullptr;
         if (cudaGetSymbolAddress(&ptr, g_noalloc_cand) != cudaSuccess || !ptr) return FS_E_CUDA;
-        int sms = 0, occ = 0;
+        int sms = 0, occ3 = 0, occ5 = 0;
         if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return FS_E_CUDA;
-        if (fs::sieve_occupancy(&occ, 3) != cudaSuccess || occ < 1) occ = 1;
+        if (fs::sieve_occupancy(&occ3, 3) != cudaSuccess || occ3 < 1) occ3 = 1;
+        if (fs::sieve_occupancy(&occ5, 5) != cudaSuccess || occ5 < 1) occ5 = 1;
         s.cand = (u64*)ptr;
         s.sm_count = sms;
-        s.blocks_per_sm = occ;
+        s.occ3 = occ3;
+        s.occ5 = occ5;
         s.ready = true;
     }
     *out = &s;
@@ -65,7 +68,8 @@ extern "C" int fs_segment_noalloc(uint64_t low, uint64_t high, uint32_t nmin, ui
                                   uint64_t deficit, fs_factor* d_hits, uint32_t hitcap, fs_counters* d_ctr,
                                   void* stream) {
     if (!d_ctr || (hitcap && !d_hits) || (nlayers && (!d_words || !d_layers4))) return FS_E_ARG;
-    if (nmin > nmax || nmax > 0x7FFFFFFFu || low < 3) return FS_E_ARG;
+    // the range checks of a search (setupSearch, cl_sieve.cpp:561-589): n from 1, p not below nmin
+    if (nmin == 0 || nmin > nmax || nmax > 0x7FFFFFFFu || low < 3 || low < nmin) return FS_E_ARG;
     if (high <= low) return FS_OK;
     if (fs_candidate_capacity(low, high) > kMaxCand) return FS_E_LIMIT;
     DeviceState* ds = nullptr;
@@ -108,8 +112,17 @@ extern "C" int fs_segment_noalloc(uint64_t low, uint64_t high, uint32_t nmin, ui
     a.hits = (fs::Factor*)d_hits;
     a.hitcap = hitcap;
     a.ctr = ctr;
-    if (fs::launch_sieve(a, fs::SETUP_PLAN, true, ds->sm_count * ds->blocks_per_sm, s, 3, fs::WALK_ANY) !=
-        cudaSuccess)
-        return FS_E_CUDA;
+    // The launch fs_search_segment would make for this segment: the walk step
+    // proven for the whole p-range with the four-candidate build (four times
+    // its resident blocks per SM, so the last wave is short), folded setup
+    // products just above 2^63, or each candidate's own step with the
+    // two-candidate build when no one step covers the range.
+    const int walk = fs::walk_for_range(low, high, nmax);
+    const int kv = walk == fs::WALK_ANY ? 3 : 5;
+    int smode = fs::SETUP_PLAN;
+    if (kv == 5 && (walk == fs::WALK_C96H || walk == fs::WALK_C96) && fs::pm_setup_for_range(low, high))
+        smode = fs::SETUP_PLAN_PM;
+    const int grid = ds->sm_count * (kv == 5 ? 4 * ds->occ5 : ds->occ3);
+    if (fs::launch_sieve(a, smode, true, grid, s, kv, walk) != cudaSuccess) return FS_E_CUDA;
     return FS_OK;
 }

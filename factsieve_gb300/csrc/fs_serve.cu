@@ -45,7 +45,7 @@ struct Job {
     State state = QUEUED;
     double t_submit = 0, t_admit = 0, t_done = 0;
     u64* d_cand = nullptr;
-    u64* d_res = nullptr;
+    u64* d_res = nullptr;      // cap residues, then cap u32 walked-n tags
     u64* d_words = nullptr;
     fs::Layer* d_layers = nullptr;
     uint32_t nlayers = 0;
@@ -113,7 +113,7 @@ const fs::SetupPlan& plan_for(Server& s, uint32_t n) {
 uint64_t job_bytes(const fs_job& j) {
     const uint64_t cap = fs_candidate_capacity(j.pmin, j.pmax);
     const uint64_t words = (uint64_t)(0.04 * j.nmin) + 64;
-    return cap * 16 + words * 8 + 4096;
+    return cap * 20 + words * 8 + 4096;
 }
 
 }  // namespace fs_serve
@@ -159,7 +159,7 @@ int admit(fs_ctx* c, Server& s, Job& j, int slot, int b, int* rc_out) {
         return 0;
     };
     if (cudaMallocAsync((void**)&j.d_cand, (j.cap + 2) * sizeof(u64), c->stream) != cudaSuccess ||
-        cudaMallocAsync((void**)&j.d_res, (j.cap + 2) * sizeof(u64), c->stream) != cudaSuccess ||
+        cudaMallocAsync((void**)&j.d_res, (j.cap + 2 + (j.cap + 1) / 2) * sizeof(u64), c->stream) != cudaSuccess ||
         cudaMallocAsync((void**)&j.d_words, (j.nwords + 2) * sizeof(u64), c->stream) != cudaSuccess ||
         cudaMallocAsync((void**)&j.d_layers, (j.nlayers + 1) * sizeof(fs::Layer), c->stream) != cudaSuccess) {
         cudaGetLastError();
@@ -355,6 +355,8 @@ extern "C" int fs_serve_round(fs_ctx* c, uint32_t* n_active, uint32_t* n_queued)
         memset(&ch, 0, sizeof(ch));
         ch.cand = j.d_cand;
         ch.residue = j.d_res;
+        ch.walked = (u32*)(j.d_res + j.cap + 2);
+        ch.nmax = j.spec.nmax;
         ch.ctr = s.d_ctr + j.slot;
         ch.words = j.d_words;
         ch.layers = j.d_layers;

@@ -620,8 +620,15 @@ __device__ __forceinline__ u32 load_quad(const u64* cand, u32 i0, u32 n, Prime (
 }
 
 // s6 + s7 of one finished candidate and its nmax round trip (check.cl:50-109).
-__device__ __forceinline__ void final_check(const Prime& c, u64 r, u32 nmax, u64& sum, u32& bad) {
-    const u64 s7 = to_mont(nmax, c);
+// n is the n the candidate's residue stands at: its walked[] tag from the
+// launches before, plus the steps of this one.  s7 = n R mod p is then
+// the reference's s7 (its Montgomery image of n, advanced by R once per step
+// across every iterate chunk, iterate.cl:67-68), and converting it back must
+// give nmax, with the reference's allowance for p <= nmax.  A chunk of n that
+// was skipped or walked twice fails the round trip and changes the checksum,
+// as it does in the reference.
+__device__ __forceinline__ void final_check(const Prime& c, u64 r, u32 n, u32 nmax, u64& sum, u32& bad) {
+    const u64 s7 = to_mont(n, c);
     u32 back = (u32)mont_mul(s7, 1, c.p, c.pinv);
     if (c.p <= nmax && nmax % c.p == back) back = nmax;
     bad += back != nmax;
@@ -645,6 +652,13 @@ __device__ __forceinline__ u64 start_residue_one(const SieveArgs& a, const Prime
     return r;
 }
 
+// The n candidate i's residue stands at when the launch starts: its tag when
+// it comes from an earlier launch (SETUP_LOAD with tags), else nstart.
+template <int SETUP>
+__device__ __forceinline__ u32 start_n(const SieveArgs& a, u32 i) {
+    return (SETUP == SETUP_LOAD && a.walked) ? a.walked[i] : a.nstart;
+}
+
 template <int SETUP, bool FINAL, int MINB, int WALK, int PPT>
 __global__ void __launch_bounds__(kSieveThreads, MINB) sieve_kernel(SieveArgs a) {
     __shared__ HitStage st;
@@ -657,6 +671,8 @@ __global__ void __launch_bounds__(kSieveThreads, MINB) sieve_kernel(SieveArgs a)
     const WalkOut o{&st, a.hits, a.hitcap, a.ctr, 0};
     u64 sum = 0;
     u32 bad = 0;
+    // every residue of the launch advances by the launch's steps
+    const u32 steps = a.nend > a.nstart ? a.nend - a.nstart : 0;
     const u32 stride = gridDim.x * blockDim.x;
     if constexpr (PPT == 4) {
         // four candidates per thread: two interleaved pairs
@@ -688,15 +704,12 @@ __global__ void __launch_bounds__(kSieveThreads, MINB) sieve_kernel(SieveArgs a)
 #pragma unroll
             for (int h = 0; h < 4; ++h) {
                 if ((u32)h >= nreal) break;
+                const u32 nw = start_n<SETUP>(a, i0 + h) + steps;
                 if (FINAL) {
-                    const u64 s7 = to_mont(a.nmax, c[h]);
-                    u32 back = (u32)mont_mul(s7, 1, c[h].p, c[h].pinv);
-                    if (c[h].p <= a.nmax && a.nmax % c[h].p == back) back = a.nmax;
-                    bad += back != a.nmax;
-                    sum += r[h] + s7;
-                    if (a.store_final) a.residue[i0 + h] = r[h];
+                    final_check(c[h], r[h], nw, a.nmax, sum, bad);
                 } else {
                     a.residue[i0 + h] = r[h];
+                    if (a.walked) a.walked[i0 + h] = nw;
                 }
             }
         }
@@ -717,26 +730,19 @@ __global__ void __launch_bounds__(kSieveThreads, MINB) sieve_kernel(SieveArgs a)
             rb = real_b ? start_residue_one<SETUP>(a, cb, ib) : ra;
         }
         walk_pair_as<WALK>(ra, rb, ca, cb, real_b, a.nstart, a.nend, o);
+        const u32 nwa = start_n<SETUP>(a, ia) + steps;
+        const u32 nwb = real_b ? start_n<SETUP>(a, ib) + steps : nwa;
         if (FINAL) {
-            // s7 = nmax*R mod p, the reference's final Montgomery image of n
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                if (h == 1 && !real_b) break;
-                const Prime& c = h ? cb : ca;
-                const u64 r = h ? rb : ra;
-                const u64 s7 = to_mont(a.nmax, c);
-                u32 back = (u32)mont_mul(s7, 1, c.p, c.pinv);
-                if (c.p <= a.nmax && a.nmax % c.p == back) back = a.nmax;
-                bad += back != a.nmax;
-                sum += r + s7;
-            }
-            if (a.store_final) {
-                a.residue[ia] = ra;
-                if (real_b) a.residue[ib] = rb;
-            }
+            // s7 from the n each walk reached, the reference's final Montgomery image of n
+            final_check(ca, ra, nwa, a.nmax, sum, bad);
+            if (real_b) final_check(cb, rb, nwb, a.nmax, sum, bad);
         } else {
             a.residue[ia] = ra;
             if (real_b) a.residue[ib] = rb;
+            if (a.walked) {
+                a.walked[ia] = nwa;
+                if (real_b) a.walked[ib] = nwb;
+            }
         }
     }
     }

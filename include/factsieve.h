@@ -13,7 +13,10 @@
  * thread-safe.  Device buffers of a search belong to the context; host
  * arrays belong to the caller.  Functions taking d_* pointers want device
  * memory the caller owns (any allocator); they run asynchronously on the
- * context's stream.
+ * context's stream.  That stream is created non-blocking: it does not wait
+ * for work on the legacy default stream, so a caller that fills a d_* buffer
+ * on another stream synchronizes first, or hands its stream to
+ * fs_set_stream.
  */
 #ifndef FACTSIEVE_H
 #define FACTSIEVE_H
@@ -198,17 +201,28 @@ int fs_serve_destroy(fs_ctx *ctx);
  * g_primecount[0]).  Only the first `cap` slots are written. */
 int fs_getsegprimes(fs_ctx *ctx, uint64_t low, uint64_t high, uint64_t *d_cand, uint32_t cap,
                     fs_counters *d_ctr);
-/* setup (setup.cl:49-103): d_residue[i] = nstart! * 2^64 mod d_cand[i] for
- * i < min(d_ctr->ncand, cap). */
+/* Walk state of the stage-level calls below.  d_residue holds
+ * FS_WALK_STATE_WORDS(cap) u64 words: the residues s6 = n! * 2^64 mod p of
+ * the cap candidates, then, as cap uint32 values starting at word cap, the n
+ * each residue stands at.  The reference keeps that n in each candidate's
+ * record as s7 = n * 2^64 mod p, advanced by 2^64 once per step
+ * (getsegprimes.cl:214-228, iterate.cl:67-68); fs_check derives s7 from it. */
+#define FS_WALK_STATE_WORDS(cap) ((uint64_t)(cap) + ((uint64_t)(cap) + 1) / 2)
+
+/* setup (setup.cl:49-103): residue i = nstart! * 2^64 mod d_cand[i] for
+ * i < min(d_ctr->ncand, cap), standing at n = nstart. */
 int fs_setup(fs_ctx *ctx, const uint64_t *d_cand, uint32_t cap, fs_counters *d_ctr, uint32_t nstart,
              uint64_t *d_residue);
-/* iterate (iterate.cl:54-80): advance residues from nstart! to nend!,
- * appending hits to d_hits at d_ctr->nhits. */
+/* iterate (iterate.cl:54-80): walk every residue through the steps
+ * n = nstart .. nend-1 (multiply by n+1, test for +-1), appending hits to
+ * d_hits at d_ctr->nhits; each residue's n advances by nend - nstart. */
 int fs_iterate(fs_ctx *ctx, const uint64_t *d_cand, uint32_t cap, fs_counters *d_ctr,
                uint64_t *d_residue, uint32_t nstart, uint32_t nend, fs_factor *d_hits,
                uint32_t hitcap);
-/* check (check.cl:50-109): add sum(s6 + s7) with s7 = nmax * 2^64 mod p to
- * d_ctr->raw_sum, flag failed nmax round trips, add the candidate count to
+/* check (check.cl:50-109): add sum(s6 + s7), s7 = n * 2^64 mod p for the n
+ * each residue stands at, to d_ctr->raw_sum; set FS_FLAG_VALIDATION unless
+ * every n equals nmax (the reference's nmax round trip, check.cl:67-78: a
+ * skipped or repeated iterate range fails it); add the candidate count to
  * d_ctr->primecount. */
 int fs_check(fs_ctx *ctx, const uint64_t *d_cand, uint32_t cap, fs_counters *d_ctr,
              const uint64_t *d_residue, uint32_t nmax);
@@ -323,6 +337,9 @@ int fs_postprocess(fs_factor *f, uint64_t n, int threads, uint64_t *kept, uint64
  *            FS_NOALLOC_MAX_CANDIDATES entries (8 MiB) that every GPU loading
  *            this library holds until the process exits.
  *
+ * The kernels and launch shapes are those fs_search_segment picks for the
+ * same segment.  The range checks of fs_search_begin apply (nmin = 0,
+ * nmin > nmax, low < nmin: FS_E_ARG).
  * A segment whose candidate bound (fs_candidate_capacity) exceeds that
  * maximum is rejected with FS_E_LIMIT before anything runs; split it.  The
  * first call on a device, with that device current, looks up the array's

@@ -23,6 +23,7 @@ def _plan_on_device(fs, nmin):
     words = np.concatenate([words, np.zeros(1, np.uint64)])   # d_words is non-null even when 2! needs no word
     dw = torch.from_numpy(words.view(np.int64).copy()).cuda()
     dl = torch.from_numpy(layers.astype(np.uint32).reshape(-1).view(np.int32).copy()).cuda()
+    torch.cuda.synchronize()
     return dw, dl, len(layers), deficit
 
 
@@ -32,6 +33,7 @@ def _candidates(ctx, lo, hi):
     cap = fs.candidate_capacity(lo, hi)
     cand = torch.zeros(cap, dtype=torch.int64, device="cuda")
     ctr = torch.zeros(4, dtype=torch.int64, device="cuda")
+    torch.cuda.synchronize()   # the library's stream does not wait for torch's fills
     ctx.getsegprimes(lo, hi, cand.data_ptr(), cap, ctr.data_ptr())
     return cand, ctr
 
@@ -68,8 +70,9 @@ def test_candidate_overflow_is_counted_and_flagged(ctx, orc):
     import factsieve_gb300 as fs
     lo, hi, cap = 1_000_000, 1_200_000, 10
     cand = torch.zeros(cap, dtype=torch.int64, device="cuda")
-    res = torch.zeros(cap, dtype=torch.int64, device="cuda")
+    res = torch.zeros(fs.walk_state_words(cap), dtype=torch.int64, device="cuda")
     ctr = torch.zeros(4, dtype=torch.int64, device="cuda")
+    torch.cuda.synchronize()
     ctx.getsegprimes(lo, hi, cand.data_ptr(), cap, ctr.data_ptr())
     want = orc.candidates(lo, hi)
     c = _counters(ctr)
@@ -152,6 +155,7 @@ def test_table_check_without_candidates_uses_a_fixed_prime(ctx, nmin):
     import torch
     cand = torch.zeros(1, dtype=torch.int64, device="cuda")
     ctr = torch.zeros(4, dtype=torch.int64, device="cuda")          # ncand = 0
+    torch.cuda.synchronize()
     direct, table = ctx.table_check(cand.data_ptr(), ctr.data_ptr(), nmin)
     q = (1 << 61) - 1
     assert direct == table == math.factorial(nmin) * (1 << 64) % q

@@ -32,9 +32,12 @@ def _torch():
 def _dev_buffers(n_cand, n_hits=1 << 16):
     torch = _torch()
     cand = torch.zeros(max(n_cand, 1), dtype=torch.int64, device="cuda")
-    res = torch.zeros(max(n_cand, 1), dtype=torch.int64, device="cuda")
+    import factsieve_gb300 as fs
+    res = torch.zeros(fs.walk_state_words(max(n_cand, 1)), dtype=torch.int64, device="cuda")
     hits = torch.zeros(max(n_hits, 1) * 2, dtype=torch.int64, device="cuda")
     ctr = torch.zeros(4, dtype=torch.int64, device="cuda")   # 32-byte fs_counters
+    # the library's stream does not wait for torch's: the zero fills must be done first
+    torch.cuda.synchronize()
     return cand, res, hits, ctr
 
 

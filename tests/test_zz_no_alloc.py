@@ -4,9 +4,10 @@ Callers that cannot allocate device memory -- code running inside a stream
 capture, services whose device memory all belongs to a pool, embedders that
 lend preallocated buffers -- call fs_segment_noalloc with their own device
 buffers; its only scratch is a fixed array compiled into the library.  Here
-it runs twice in a row on one stream, with no synchronisation between the
-calls (so the second call starts on the first call's leftovers in that
-array), and each result must equal the allocating entry point's exactly:
+it runs six segments in a row on one stream (p from 1e6 to just below 2^64),
+with no synchronisation between the calls (so each call starts on the
+previous call's leftovers in that array), and each result must equal the
+allocating entry point's exactly:
 same hit list, same sum of (s6 + s7), same candidate count (integer work, so
 the tolerance is zero).  This file is collected last on purpose.
 """
@@ -21,6 +22,11 @@ SEGMENTS = [
     # (low, high, nmin, nmax): a small-p segment with many hits, then a large-p one
     (1_000_000, 1_400_000, 1000, 2600),
     (1_000_000_000_000, 1_000_004_000_000, 100_000, 101_000),
+    # p crossing 2^32, and near 2^62, 2^63 (folded setup products) and 2^64 - 1
+    ((1 << 32) - 2_000_000, (1 << 32) + 2_000_000, 5_000, 5_400),
+    ((1 << 62) - 3_000_000, (1 << 62) + 1_000_000, 100_000, 100_300),
+    ((1 << 63) + 1, (1 << 63) + 3_000_001, 1_000_000, 1_000_200),
+    ((1 << 64) - 4_000_000, (1 << 64) - 1, 20_000, 20_200),
 ]
 
 
@@ -90,3 +96,23 @@ def test_noalloc_rejects_a_segment_beyond_its_scratch():
     rc = f(low, high, 1000, 2000, None, None, 0, 0, None, 0, ctr.data_ptr(), None)
     assert rc == 10   # FS_E_LIMIT
     assert fs.lib().fs_strerror(rc).decode() == "request exceeds a fixed size limit"
+
+
+@pytest.mark.parametrize("low,high,nmin,nmax", [
+    (1_000_000, 1_100_000, 0, 1000),       # nmin = 0
+    (1_000_000, 1_100_000, 2000, 1000),    # nmin > nmax
+    (1_000_000, 1_100_000, 2_000_000, 2_000_100),   # p below nmin
+])
+def test_noalloc_rejects_what_a_search_rejects(low, high, nmin, nmax):
+    """The range checks of fs_search_begin (the reference's setupSearch,
+    cl_sieve.cpp:561-589) apply: FS_E_ARG, and nothing runs."""
+    import torch
+    import factsieve_gb300 as fs
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    f = _entry(fs)
+    ctr = torch.zeros(4, dtype=torch.int64, device="cuda")
+    rc = f(low, high, nmin, nmax, None, None, 0, 0, None, 0, ctr.data_ptr(), None)
+    assert rc == 1   # FS_E_ARG
+    torch.cuda.synchronize()
+    assert int(ctr.abs().sum()) == 0
