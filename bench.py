@@ -7,8 +7,11 @@ Workload (default config2, the plain large sieve): p in [1e12, 1e12 + 1e9),
 n in [1e5, 2e5).  One step = one pass over the whole p-range as one segment
 (the command line's default segment width; wider segments leave a shorter
 partial last wave), run through getsegprimes -> setup -> iterate -> check.
-Config 3 steps are 1e8-wide segments (its measured best); --segment
-overrides the width (the ncu full capture uses 1e8).
+Config 3 passes run as 1e8-wide segments (its measured best); --segment
+overrides the width (the ncu full capture uses 1e8).  After the timed
+region, a one-GPU config2 run adds sub-objects for config 1 (end to end,
+against its fixture), config 3 (one timed pass, roofline, e2e) and config 4
+(the 64-job batch against 64 sequential plain runs); --no-extra skips them.
 Metric: (p,n) pair-steps/s = candidates x (nmax - nmin) / time, plus the
 fraction of the integer-multiply roofline.
 
@@ -28,8 +31,11 @@ fraction of the integer-multiply roofline.
   cpu_baseline  the CPU oracle (OpenMP over all host cores, the reference's
              algorithm restated) on a bounded slice of the same workload.
 
-With --gpus N (torchrun, one rank per GPU) the p-segments are dealt
-round-robin to the ranks: no data-path collective, weak scaling.
+With --gpus N (torchrun, one rank per GPU) each rank takes a contiguous
+share of the p-range (strong scaling: the whole range is one step at every
+N); nothing crosses ranks on the data path, and the shares' raw sums and
+candidate counts, added on the host, must equal the oracle fixture of the
+whole range (the line's combined_check).
 
 --impl reference times the reference's algorithm on the host CPU (the
 oracle port: the reference's own GPU path is OpenCL and has no runtime
@@ -56,13 +62,17 @@ WORKLOADS = {
     "config3": (1 << 63, (1 << 63) + 1_000_000_000, 1_000_000, 1_010_000, 100_000_000),
 }
 IMAD_PER_PRODUCT = 20   # reference m_mul on 32-bit limbs (8 mul_wide + 4 + 8)
-# DRAM bytes (read + write) per sieve launch and IMAD-pipe busy share from
-# one ncu --set full capture of one launch of the same workload
-# (profiles/sieve_kernel_config2.md, profiles/sieve_kernel_config3.md)
+# DRAM bytes (read + write) per sieve launch and the integer-multiply pipe's
+# busy share, from one `ncu --set full --clock-control none` capture of the
+# fused sieve kernel on the same workload (dram__bytes_read.sum +
+# dram__bytes_write.sum; sm__pipe_fmaheavy_cycles_active): config 2 captured
+# on a 1e8-wide segment (29,120,512 B) and scaled by 10 to the whole-range
+# launch the bench times, config 3 on one of its 1e8-wide launches.
 NCU_CAPTURE = {
-    # config 2: a 1e8-wide capture (29,120,512 B) scaled by 10 to the whole-range launch the bench times
-    "config2": {"traffic": 291_205_120, "imad_pipe_busy": 0.773, "source": "profiles/sieve_kernel_config2.md"},
-    "config3": {"traffic": 18_765_568, "imad_pipe_busy": 0.836, "source": "profiles/sieve_kernel_config3.md"},
+    "config2": {"traffic": 291_205_120, "imad_pipe_busy": 0.773,
+                "source": "ncu --set full capture of sieve_kernel, bench.py --segment 1e8"},
+    "config3": {"traffic": 18_765_568, "imad_pipe_busy": 0.836,
+                "source": "ncu --set full capture of sieve_kernel, bench.py --workload config3"},
 }
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 
@@ -350,9 +360,20 @@ def run_reference(args):
 
 # ------------------------------------------------------------ GPU leg -----
 
+def fixture(wl):
+    """The oracle's result for the whole workload range (tests/golden/run_<wl>.json)."""
+    try:
+        with open(os.path.join(GOLDEN, f"run_{wl}.json")) as fh:
+            d = json.load(fh)
+    except OSError:
+        return None
+    return {"raw_sum": int(d["raw_sum"], 16), "primecount": int(d["primecount"])}
+
+
 def run_ours(args):
     import torch
     import factsieve_gb300 as fs
+    from factsieve_gb300.shard import shard_bounds
     ws, rank, local = dist_env()
     if ws > 1:
         torch.cuda.set_device(local)
@@ -363,23 +384,23 @@ def run_ours(args):
     if args.segment:
         seg = int(args.segment)
     W = nmax - nmin
-    nseg = (pmax - pmin + seg - 1) // seg
-
-    def seg_range(i):
-        lo = pmin + (i % nseg) * seg
-        return lo, min(lo + seg, pmax)
+    # my contiguous share of the whole range; one step = my share, as segments of width seg
+    lo, hi = shard_bounds(pmin, pmax, ws, rank)
+    segs = [(a, min(a + seg, hi)) for a in range(lo, hi, seg)]
 
     ctx = fs.Context(dev)
     stream = torch.cuda.Stream(device=dev)
     ctx.set_stream(stream.cuda_stream)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)   # > 129 MB L2
 
-    # my segments: round-robin over ranks, K timed after W warm-up
-    mine = [rank + ws * j for j in range(args.warmup + args.steps)]
+    def one_step():
+        for s_lo, s_hi in segs:
+            ctx.segment(s_lo, s_hi)
+
     ctx.begin(pmin, pmax, nmin, nmax)
     with torch.cuda.stream(stream):
-        for i in mine[: args.warmup]:
-            ctx.segment(*seg_range(i))
+        for _ in range(args.warmup):
+            one_step()
             flush.fill_(1)
     cap = 30_000_000 if pmin < 0xFFFFFFFF else 1_000_000
     ctx.collect(cap)                       # drain warm-up work and counters
@@ -392,8 +413,8 @@ def run_ours(args):
     with ClockSampler(dev) as clk:
         with torch.cuda.stream(stream):
             e0.record(stream)
-            for j, i in enumerate(mine[args.warmup:]):
-                ctx.segment(*seg_range(i))
+            for j in range(args.steps):
+                one_step()
                 if j + 1 < args.steps:
                     flush.fill_(j & 0xFF)  # L2 flush between timed steps
             e1.record(stream)
@@ -403,69 +424,96 @@ def run_ours(args):
     ctx.set_timing(False)
     hits, raw, primecount, flags, rc = ctx.collect(cap)
     assert rc == 0, f"device flagged {flags}"
+    my_pc = primecount
     pairs = primecount * W
-    # max time over ranks, total work over ranks
+    # max time over ranks, total work over ranks; the shares' sums combine on the host
+    # (u64 adds), and K passes over the whole range must give K times its oracle result
+    shares = [(raw, primecount)]
     if dist:
-        t = torch.tensor([ms, float(pairs), st["sieve_ms"], float(st["sieve_launches"]), float(primecount)],
-                         dtype=torch.float64, device=dev)
+        t = torch.tensor([ms, float(pairs)], dtype=torch.float64, device=dev)
         tmax = t.clone()
         dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
         tsum = t.clone()
         dist.all_reduce(tsum, op=dist.ReduceOp.SUM)
         ms, pairs = tmax[0].item(), tsum[1].item()
-        primecount = int(tsum[4].item())
+        shares = [None] * ws
+        dist.all_gather_object(shares, (raw, primecount))
+    M = (1 << 64) - 1
+    comb_raw = sum(r for r, _ in shares) & M
+    comb_pc = sum(c for _, c in shares)
+    primecount = comb_pc
+    want = fixture(wl)
+    check = None
+    if want:
+        K = args.steps
+        check = {"combined_raw_sum": f"{comb_raw:016X}", "combined_primecount": comb_pc,
+                 "expected_raw_sum": f"{(want['raw_sum'] * K) & M:016X}",
+                 "expected_primecount": want["primecount"] * K,
+                 "source": f"tests/golden/run_{wl}.json (oracle), times {K} timed passes",
+                 "equal": comb_raw == (want["raw_sum"] * K) & M and comb_pc == want["primecount"] * K}
     value = pairs / (ms * 1e-3)
 
     # roofline of the dominant kernel, from this rank's events
-    my_pc = primecount if not dist else int(t[4].item())
     roof = roofline(ctx, fs, wl, my_pc, st, ms, clk.summary(), seg)
-
-    # e2e through the public API with host buffers, on rank 0's first segments
-    e2e = None
-    if rank == 0:
-        e2e_steps = max(1, min(args.steps, 3))
-        ctx.set_stream(None)
-        words, layers, _ = fs.setup_plan(nmin)          # the plan each call uploads (bytes counted below)
-        plan_bytes = words.nbytes + layers.nbytes
-        t0 = time.perf_counter()
-        e2e_pairs = 0
-        h2d = d2h = 0
-        for i in range(e2e_steps):
-            lo, hi = seg_range(i)
-            r = ctx.sieve(lo, hi, nmin, nmax, threads=os.cpu_count() or 2)
-            e2e_pairs += r.primecount * W
-            h2d += plan_bytes + 64
-            d2h += 32 + 16 * r.nhits
-        dt = time.perf_counter() - t0
-        e2e = {"value": e2e_pairs / dt, "unit": "pair-steps/s", "h2d_bytes_per_step": h2d // e2e_steps,
-               "d2h_bytes_per_step": d2h // e2e_steps, "steps": e2e_steps,
-               "path": "Context.sieve (fs_search_begin/segment/collect + fs_postprocess)"}
-
-    if e2e:
-        # the reference accounting end to end: e2e pair-steps/s with each step's
-        # share of the reference's setup and check products
-        ref = roof["reference_mulmod_roofline"]
-        per_step = (W + reference_setup_products(nmin) + 1) / W
-        ref["end_to_end_frac"] = e2e["value"] * per_step / (ref["peak"] * 1e9) if ref["peak"] else None
+    # e2e through the public API with host buffers: every rank searches its
+    # whole share with Context.sieve per step (plan upload, counters and hits
+    # back, CPU verification), wall clock, max over ranks
+    e2e_steps = max(1, min(args.steps, 3))
+    ctx.set_stream(None)
+    words, layers, _ = fs.setup_plan(nmin)          # the plan each call uploads (bytes counted below)
+    plan_bytes = words.nbytes + layers.nbytes
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    e2e_pairs = 0
+    h2d = d2h = 0
+    for _ in range(e2e_steps):
+        r = ctx.sieve(lo, hi, nmin, nmax, threads=os.cpu_count() or 2)
+        e2e_pairs += r.primecount * W
+        h2d += plan_bytes + 64
+        d2h += 32 + 16 * r.nhits
+    dt = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([dt, float(e2e_pairs)], dtype=torch.float64, device=dev)
+        tmax, tsum = t.clone(), t.clone()
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        dist.all_reduce(tsum, op=dist.ReduceOp.SUM)
+        dt, e2e_pairs = tmax[0].item(), tsum[1].item()
+    e2e = {"value": e2e_pairs / dt, "unit": "pair-steps/s", "h2d_bytes_per_step": h2d // e2e_steps,
+           "d2h_bytes_per_step": d2h // e2e_steps, "steps": e2e_steps,
+           "path": "Context.sieve (fs_search_begin/segment/collect + fs_postprocess) on each rank's share"}
+    # the reference accounting end to end: e2e pair-steps/s with each step's
+    # share of the reference's setup and check products
+    ref = roof["reference_mulmod_roofline"]
+    per_step = (W + reference_setup_products(nmin) + 1) / W
+    ref["end_to_end_frac"] = e2e["value"] * per_step / ws / (ref["peak"] * 1e9) if ref["peak"] else None
 
     if rank == 0:
         cpu = cpu_baseline(wl) if (ws == 1 and not args.no_cpu) else None
         line = {
             "metric": "(p,n) pair-steps/sec", "value": value, "unit": "pair-steps/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "u64",
             "data": "synthetic (integer ranges; no dataset)",
             "config": {"workload": f"{wl}: p in [{pmin}, {pmax}), n in [{nmin}, {nmax})",
-                       "step": f"one p-segment of {seg} (segment i of {nseg}, dealt round-robin to ranks)",
-                       "parallelism": f"p-segments over {ws} GPU(s), no collective",
+                       "step": f"one pass over the whole p-range: each rank its contiguous share, as "
+                               f"{len(segs)} segment(s) of up to {seg}",
+                       "parallelism": f"contiguous p-shares over {ws} GPU(s), no collective on the data path; "
+                                      f"the shares' sums combine on the host",
                        "l2": "flushed between timed steps (256 MiB write)",
                        "candidates_timed": primecount, "pair_steps_timed": pairs},
+            "combined_check": check,
             "roofline": roof,
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": int(st["launches"]),
             "clocks": clk.summary(),
         }
+        if ws == 1 and wl == "config2" and not args.no_extra:
+            # the other single-GPU configurations, after the timed region
+            line["config1"] = extra_config1(ctx, fs)
+            line["config3"] = extra_config3(ctx, fs, torch, dev)
+            line["config4"] = batch_compare(ctx, fs, torch, dev, load_jobs(), warmup=1)
         print(json.dumps(line), flush=True)
     ctx.close()
     if dist:
@@ -474,27 +522,92 @@ def run_ours(args):
     return 0
 
 
+def extra_config1(ctx, fs):
+    """Config 1 (p in [1e6, 2e6), n in [1000, 2000)) through Context.sieve,
+    wall clock, against its oracle fixture."""
+    pmin, pmax, nmin, nmax, _ = WORKLOADS["config1"]
+    ctx.set_stream(None)
+    ctx.sieve(pmin, pmax, nmin, nmax)                  # warm-up
+    t0 = time.perf_counter()
+    r = ctx.sieve(pmin, pmax, nmin, nmax, threads=os.cpu_count() or 2)
+    dt = time.perf_counter() - t0
+    with open(os.path.join(GOLDEN, "run_config1.json")) as fh:
+        want = json.load(fh)
+    return {"workload": f"config1: p in [{pmin}, {pmax}), n in [{nmin}, {nmax})",
+            "e2e_pair_steps_per_s": r.primecount * (nmax - nmin) / dt, "wall_s": dt,
+            "primecount": r.primecount, "factorcount": r.factorcount, "checksum": f"{r.checksum:016X}",
+            "equals_oracle_fixture": (r.primecount, r.factorcount, f"{r.checksum:016X}") ==
+                                     (want["primecount"], want["factorcount"], want["checksum"])}
+
+
+def extra_config3(ctx, fs, torch, dev):
+    """Config 3 (p in [2^63, 2^63 + 1e9), n in [1e6, 1.01e6)): one untimed and
+    one timed pass over the whole range as 1e8-wide segments on the library's
+    stream (CUDA events around the pass and around each sieve launch), the
+    kernel's roofline against its ceilings, and one 1e8-wide segment end to end
+    through Context.sieve."""
+    wl = "config3"
+    pmin, pmax, nmin, nmax, seg = WORKLOADS[wl]
+    W = nmax - nmin
+    segs = [(a, min(a + seg, pmax)) for a in range(pmin, pmax, seg)]
+    stream = torch.cuda.Stream(device=dev)
+    ctx.set_stream(stream.cuda_stream)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    ctx.begin(pmin, pmax, nmin, nmax)
+    with torch.cuda.stream(stream):
+        for s_lo, s_hi in segs:
+            ctx.segment(s_lo, s_hi)
+        flush.fill_(3)
+    ctx.collect(1 << 20)
+    ctx.reset_stats()
+    ctx.set_timing(True)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev) as clk:
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for s_lo, s_hi in segs:
+                ctx.segment(s_lo, s_hi)
+            e1.record(stream)
+        torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1)
+    st = ctx.stats()
+    ctx.set_timing(False)
+    _, raw, pc, flags, rc = ctx.collect(1 << 20)
+    want = fixture(wl)
+    roof = roofline(ctx, fs, wl, pc, st, ms, clk.summary(), seg)
+    ctx.set_stream(None)
+    t0 = time.perf_counter()
+    r = ctx.sieve(segs[0][0], segs[0][1], nmin, nmax, threads=os.cpu_count() or 2)
+    dt = time.perf_counter() - t0
+    return {"workload": f"config3: p in [{pmin}, {pmax}), n in [{nmin}, {nmax})",
+            "value": pc * W / (ms * 1e-3), "unit": "pair-steps/s", "ms_per_pass": ms,
+            "step": f"one pass over the whole range as {len(segs)} segments of {seg}",
+            "equals_oracle_fixture": (raw, pc, rc) == (want["raw_sum"], want["primecount"], 0) if want else None,
+            "roofline": {k: roof[k] for k in ("bound", "achieved", "peak", "unit", "frac", "kernel_ms_per_launch",
+                                              "walk_step", "setup_product", "setup_products_per_candidate",
+                                              "ceilings")},
+            "e2e": {"value": r.primecount * W / dt, "unit": "pair-steps/s", "wall_s": dt,
+                    "path": f"Context.sieve over [{segs[0][0]}, {segs[0][1]})"},
+            "clocks": clk.summary()}
+
+
 def load_jobs():
     with open(os.path.join(GOLDEN, "jobs_config4.json")) as fh:
         return [tuple(j) for j in json.load(fh)["jobs"]]
 
 
-def run_batch(args):
-    """Config 4: 64 uneven jobs (seed 1) in one persistent, graph-captured
+def batch_compare(ctx, fs, torch, dev, jobs, warmup=3):
+    """Config 4: the 64 uneven jobs (seed 1) in one persistent, graph-captured
     launch against the same 64 jobs run one after another through the plain
     path on the same GPU.  Both legs are timed with CUDA events on the
     library's stream (device time) and with the wall clock; every job's
     (primecount, raw sum, hits) must agree between the legs."""
-    import torch
-    import factsieve_gb300 as fs
-    jobs = load_jobs()
-    dev = torch.cuda.current_device()
-    ctx = fs.Context(dev)
     stream = torch.cuda.Stream(device=dev)
     ctx.set_stream(stream.cuda_stream)
     cap = 1 << 20
     small = [(p0, p0 + max(10_000, (p1 - p0) // 200), n0, n1) for p0, p1, n0, n1 in jobs]
-    for _ in range(args.warmup):                  # warm-up: the same mix at 1/200 of the p-widths
+    for _ in range(warmup):                       # warm-up: the same mix at 1/200 of the p-widths
         ctx.batch_sieve(small)
     # batched leg
     ctx.batch_prepare(jobs, hitcap=cap)
@@ -527,25 +640,40 @@ def run_batch(args):
     wall_p = time.perf_counter() - t0
     sp = ctx.stats()
     ctx.set_timing(False)
+    ctx.set_stream(None)
     dev_p = (sp["sieve_ms"] + sp["gen_ms"]) * 1e-3
     same = True
     for k, (r, pl) in enumerate(zip(res, plain)):
         mine = sorted(zip(hits["p"][hits["pad"] == k].tolist(), hits["nc"][hits["pad"] == k].tolist()))
         same &= (r["primecount"], r["raw_sum"], mine) == pl
+    return {"workload": "config4: 64 uneven jobs in one persistent launch (tests/golden/jobs_config4.json)",
+            "pair_steps": pairs, "value": pairs / dev_b, "unit": "pair-steps/s",
+            "batched": {"device_s": dev_b, "wall_s": wall_b, "pair_steps_per_s": pairs / dev_b,
+                        "wall_pair_steps_per_s": pairs / wall_b, "launches": int(st["launches"])},
+            "plain_sequential": {"device_s": dev_p, "wall_s": wall_p, "pair_steps_per_s": pairs / dev_p,
+                                 "wall_pair_steps_per_s": pairs / wall_p, "launches": int(sp["launches"])},
+            "speedup_device": dev_p / dev_b, "speedup_wall": wall_p / wall_b,
+            "per_job_bit_exact": bool(same), "warmup": "the same 64 jobs at 1/200 of their p-widths",
+            "clocks": clk.summary()}
+
+
+def run_batch(args):
+    """Config 4 as its own line (batch_compare)."""
+    import torch
+    import factsieve_gb300 as fs
+    dev = torch.cuda.current_device()
+    ctx = fs.Context(dev)
+    b = batch_compare(ctx, fs, torch, dev, load_jobs(), warmup=args.warmup)
     line = {
-        "metric": "(p,n) pair-steps/sec", "value": pairs / dev_b, "unit": "pair-steps/s", "n_gpus": 1,
-        "steps": 1, "warmup": args.warmup, "ms_per_step": dev_b * 1e3, "higher_is_better": True,
+        "metric": "(p,n) pair-steps/sec", "value": b["value"], "unit": "pair-steps/s", "n_gpus": 1,
+        "steps": 1, "warmup": args.warmup, "ms_per_step": b["batched"]["device_s"] * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic (64 jobs, seed 1)",
-        "config": {"workload": "config4: 64 uneven jobs in one persistent launch (tests/golden/jobs_config4.json)",
-                   "warmup": "the same 64 jobs at 1/200 of their p-widths", "pair_steps": pairs},
-        "batched": {"device_s": dev_b, "wall_s": wall_b, "pair_steps_per_s": pairs / dev_b,
-                    "wall_pair_steps_per_s": pairs / wall_b},
-        "plain_sequential": {"device_s": dev_p, "wall_s": wall_p, "pair_steps_per_s": pairs / dev_p,
-                             "wall_pair_steps_per_s": pairs / wall_p},
-        "speedup_device": dev_p / dev_b, "speedup_wall": wall_p / wall_b,
-        "per_job_bit_exact": bool(same),
-        "gpu_launches": int(st["launches"]),
-        "clocks": clk.summary(),
+        "config": {"workload": b["workload"], "warmup": b["warmup"], "pair_steps": b["pair_steps"]},
+        "batched": b["batched"], "plain_sequential": b["plain_sequential"],
+        "speedup_device": b["speedup_device"], "speedup_wall": b["speedup_wall"],
+        "per_job_bit_exact": b["per_job_bit_exact"],
+        "gpu_launches": b["batched"]["launches"],
+        "clocks": b["clocks"],
     }
     print(json.dumps(line), flush=True)
     ctx.close()
@@ -624,6 +752,8 @@ def main():
     ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS) + ["config4", "config5"])
     ap.add_argument("--serve-seconds", type=float, default=180.0, help="config5: stop the replay after this long")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="config2 at one GPU: skip the config1/config3/config4 sub-objects after the timed region")
     ap.add_argument("--segment", type=float, default=0,
                     help="p-width of one step (default: the workload's; e.g. 1e8 for a short profiling case)")
     args = ap.parse_args()

@@ -125,12 +125,14 @@ int main(int argc, char* argv[]) {
 
     int ndev = 0;
     if (fs_device_count(&ndev) != FS_OK || ndev <= so.device) {
+        // reported here; the run fails when it first needs the device, after
+        // the checkpoint files are read (a finished workunit needs none)
         printf("No CUDA device %d available.\n", so.device);
         fprintf(stderr, "Error: no CUDA device %d available\n", so.device);
-        return EXIT_FAILURE;
+    } else {
+        fprintf(stderr, "GPU Info:\n  CUDA device: \t\t%d of %d\n", so.device, ndev);
+        printf("GPU Info:\n  CUDA device: \t\t%d of %d\n", so.device, ndev);
     }
-    fprintf(stderr, "GPU Info:\n  CUDA device: \t\t%d of %d\n", so.device, ndev);
-    printf("GPU Info:\n  CUDA device: \t\t%d of %d\n", so.device, ndev);
     const int rc = so.test ? run_self_test(st, so) : run_search(st, so);
     return rc ? EXIT_FAILURE : EXIT_SUCCESS;
 }

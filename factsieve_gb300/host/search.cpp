@@ -324,17 +324,8 @@ int truncate_results() {
 
 int run_search(WorkStatus& st, SearchOptions& so) {
     if (setup_search(st, so)) return EXIT_FAILURE;
-    fs_ctx* ctx = nullptr;
-    int rc = fs_create(so.device, &ctx);
-    if (rc) {
-        both("Error: cannot open CUDA device %d: %s\n", so.device, fs_strerror(rc));
-        return EXIT_FAILURE;
-    }
-    struct Closer {
-        fs_ctx* c;
-        ~Closer() { fs_destroy(c); }
-    } closer{ctx};
-
+    // checkpoint and results file first (cl_sieve.cpp:998-1024): a finished
+    // workunit or an unwritable factors.txt needs no device
     if (so.test) {
         if (truncate_results()) return EXIT_FAILURE;
     } else if (read_state(st, so)) {
@@ -348,6 +339,17 @@ int run_search(WorkStatus& st, SearchOptions& so) {
         if (truncate_results()) return EXIT_FAILURE;
         st.last_trickle = (uint64_t)time(nullptr);
     }
+
+    fs_ctx* ctx = nullptr;
+    int rc = fs_create(so.device, &ctx);
+    if (rc) {
+        both("Error: cannot open CUDA device %d: %s\n", so.device, fs_strerror(rc));
+        return EXIT_FAILURE;
+    }
+    struct Closer {
+        fs_ctx* c;
+        ~Closer() { fs_destroy(c); }
+    } closer{ctx};
 
     if ((rc = fs_search_begin(ctx, st.pmin, st.pmax, st.nmin, st.nmax, so.numresults))) {
         both("error: %s %s\n", fs_strerror(rc), fs_last_error(ctx));

@@ -138,7 +138,7 @@ typedef struct {
 
 /* Prepare a batch: build every job's setup plan, size its candidate buffer
  * and capture the whole batch -- counter clears, one candidate launch per job
- * and one persistent sieve launch whose blocks take (job, 512-candidate) tiles
+ * and one persistent sieve launch whose blocks take (job, 1024-candidate) tiles
  * from a global queue, heaviest jobs first -- into a CUDA graph.  Replaces any
  * previous batch of the context.  Each job's results are bit-identical to a
  * search of that job alone.  No counterpart in the reference, which runs one

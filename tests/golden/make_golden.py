@@ -11,8 +11,9 @@ device-side quantities (sum of s6+s7, hit count) and the kept factor list
 The five self-test ranges and their golden triples are the reference's own
 (cl_sieve.cpp:1283-1364); the script refuses to write a self-test fixture
 whose triple disagrees with them, so every fixture derived from the oracle
-comes from an oracle pinned to the reference.  The BASELINE workloads
-(config 1-3) have no reference goldens: their fixtures are oracle output.
+comes from an oracle pinned to the reference.  The benchmark workloads
+(config 1-3: the plain small, plain large and top-of-u64 sieves) have no
+reference goldens: their fixtures are oracle output.
 
 Also writes candidates_small.json: exact candidate lists (reference
 getsegprimes semantics) for a few short p-ranges, used by the GPU parity

@@ -80,6 +80,42 @@ def test_cli_resumes_from_checkpoint(fslib, orc, tmp_path):
     assert (tmp_path / "factors.txt").read_text().splitlines() == g["factors"] + [g["checksum"]]
 
 
+def test_cli_resumes_after_a_kill_between_checkpoint_writes(fslib, orc, tmp_path):
+    """Killed while writing the newer checkpoint: stateB.ckp is cut short and
+    stateA.ckp holds the last complete one (p = mid).  The run resumes from
+    stateA.ckp and ends with the uninterrupted run's factors.txt and checksum."""
+    g = _gold("config1")
+    mid = 1_500_000
+    part = orc.run(g["pmin"], mid, g["nmin"], g["nmax"])
+    lines = [f"{int(p)} | {abs(int(nc))}!{'+1' if nc > 0 else '-1'}"
+             for p, nc in zip(part["factors"]["p"], part["factors"]["nc"])]
+    (tmp_path / "factors.txt").write_text("".join(l + "\n" for l in lines))
+    (tmp_path / "stateA.ckp").write_bytes(_state(g["pmin"], g["pmax"], mid, part["checksum"], part["primecount"],
+                                                 part["factorcount"], g["nmin"], g["nmax"]))
+    newer = _state(g["pmin"], g["pmax"], 1_800_000, 1, 2, 3, g["nmin"], g["nmax"])
+    (tmp_path / "stateB.ckp").write_bytes(newer[:50])
+    r = _cli(fslib, _args(g), tmp_path)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Cannot parse stateB.ckp !!!" in r.stdout
+    assert "Resuming from checkpoint in stateA.ckp" in r.stdout
+    assert (tmp_path / "factors.txt").read_text().splitlines() == g["factors"] + [g["checksum"]]
+
+
+@pytest.mark.parametrize("name", ["config1", "near_2p62"])
+def test_cli_full_disk_on_factors_file(fslib, tmp_path, name):
+    """factors.txt on a full disk (/dev/full: opens, every write fails): the
+    factor lines (config 1) or the final checksum line (a range without
+    factors) cannot be written, and the run ends with EXIT_FAILURE and the
+    reference's message (cl_sieve.cpp:539-541, 758-768)."""
+    if not os.path.exists("/dev/full"):
+        pytest.skip("no /dev/full")
+    g = _gold(name)
+    os.symlink("/dev/full", tmp_path / "factors.txt")
+    r = _cli(fslib, _args(g), tmp_path)
+    assert r.returncode == 1, r.stdout + r.stderr
+    assert "Cannot write to factors.txt !!!" in r.stderr
+
+
 def test_cli_ignores_corrupt_checkpoint(fslib, tmp_path):
     g = _gold("config1")
     (tmp_path / "stateA.ckp").write_bytes(_state(g["pmin"], g["pmax"], 1_500_000, 5, 7, 0, g["nmin"], g["nmax"],

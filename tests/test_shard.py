@@ -1,7 +1,7 @@
-"""Multi-rank path on CPU: world-size-2 gloo groups shard one search over p,
-each rank computes its shard with the oracle, and the host combine equals the
-single-rank search bit for bit.  A failing rank surfaces as an error on the
-other rank, not a hang."""
+"""Multi-rank path: world-size-2 gloo groups shard one search over p, each
+rank computes its shard (with the oracle on CPU, or on the GPU under -m gpu),
+and the host combine equals the single-rank search bit for bit.  A failing
+rank surfaces as an error on the other rank, not a hang."""
 import os
 import socket
 
@@ -31,7 +31,7 @@ def _oracle_compute(nmin, nmax):
     return run
 
 
-def _worker(rank, world, port, job, fail_rank, out):
+def _worker(rank, world, port, job, fail_rank, out, gpu=False):
     import sys
     sys.path.insert(0, ROOT)
     import datetime
@@ -41,7 +41,7 @@ def _worker(rank, world, port, job, fail_rank, out):
                             timeout=datetime.timedelta(seconds=20))
     try:
         pmin, pmax, nmin, nmax = job
-        compute = _oracle_compute(nmin, nmax)
+        compute = None if gpu else _oracle_compute(nmin, nmax)   # None: this rank's GPU (Context.sieve)
         if rank == fail_rank:
             def compute(lo, hi):
                 raise RuntimeError("injected failure on this rank")
@@ -57,12 +57,12 @@ def _worker(rank, world, port, job, fail_rank, out):
             pass
 
 
-def _run(world, job, fail_rank=-1):
+def _run(world, job, fail_rank=-1, gpu=False):
     ctx = mp.get_context("spawn")
     mgr = ctx.Manager()
     out = mgr.dict()
     port = _free_port()
-    procs = [ctx.Process(target=_worker, args=(r, world, port, job, fail_rank, out)) for r in range(world)]
+    procs = [ctx.Process(target=_worker, args=(r, world, port, job, fail_rank, out, gpu)) for r in range(world)]
     for p in procs:
         p.start()
     for p in procs:
@@ -81,6 +81,23 @@ def test_two_rank_shards_combine_to_the_whole_search(orc):
         assert r[0] == "ok", r
         assert (r[1], r[2], r[3]) == (whole["primecount"], whole["checksum"], whole["factorcount"])
         assert r[4] == [(int(p), int(nc)) for p, nc in zip(whole["factors"]["p"], whole["factors"]["nc"])]
+
+
+@pytest.mark.gpu
+def test_two_rank_gpu_shards_combine_to_the_whole_search(orc):
+    """The same with each rank searching its shard on the GPU (sieve_distributed's
+    default compute).  This run has one GPU, so both ranks share cuda:0; their
+    kernels are independent (nothing on the device waits for the other rank)."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    job = (1_000_000_000_000, 1_000_002_000_000, 100_000, 101_000)
+    whole = orc.run(*job)
+    res = _run(2, job, gpu=True)
+    assert set(res) == {0, 1}
+    for r in res.values():
+        assert r[0] == "ok", r
+        assert (r[1], r[2], r[3]) == (whole["primecount"], whole["checksum"], whole["factorcount"])
 
 
 def test_failed_rank_is_reported_not_hung():
