@@ -397,6 +397,9 @@ def run_ours(args):
         for s_lo, s_hi in segs:
             ctx.segment(s_lo, s_hi)
 
+    # the launch shape: measured on a sample of this rank's share by the
+    # library's tuner (fs_autotune) and applied to the context
+    tune = ctx.autotune(lo, hi, nmin, nmax)
     ctx.begin(pmin, pmax, nmin, nmax)
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
@@ -503,6 +506,8 @@ def run_ours(args):
                        "l2": "flushed between timed steps (256 MiB write)",
                        "candidates_timed": primecount, "pair_steps_timed": pairs},
             "combined_check": check,
+            "tuning": {"shape": tune["tuning"], "sample_rate_pair_steps_per_s": tune["rate"],
+                       "shapes_tried": tune["shapes_tried"], "by": "fs_autotune on a sample of the share"},
             "roofline": roof,
             "cpu_baseline": cpu,
             "e2e": e2e,
@@ -527,6 +532,7 @@ def extra_config1(ctx, fs):
     wall clock, against its oracle fixture."""
     pmin, pmax, nmin, nmax, _ = WORKLOADS["config1"]
     ctx.set_stream(None)
+    ctx.set_tuning()                                   # default shapes (too small a run to time)
     ctx.sieve(pmin, pmax, nmin, nmax)                  # warm-up
     t0 = time.perf_counter()
     r = ctx.sieve(pmin, pmax, nmin, nmax, threads=os.cpu_count() or 2)
@@ -553,6 +559,7 @@ def extra_config3(ctx, fs, torch, dev):
     stream = torch.cuda.Stream(device=dev)
     ctx.set_stream(stream.cuda_stream)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    tune = ctx.autotune(pmin, pmax, nmin, nmax)
     ctx.begin(pmin, pmax, nmin, nmax)
     with torch.cuda.stream(stream):
         for s_lo, s_hi in segs:
@@ -589,6 +596,7 @@ def extra_config3(ctx, fs, torch, dev):
                                               "ceilings")},
             "e2e": {"value": r.primecount * W / dt, "unit": "pair-steps/s", "wall_s": dt,
                     "path": f"Context.sieve over [{segs[0][0]}, {segs[0][1]})"},
+            "tuning": {"shape": tune["tuning"], "shapes_tried": tune["shapes_tried"]},
             "clocks": clk.summary()}
 
 
@@ -609,6 +617,8 @@ def batch_compare(ctx, fs, torch, dev, jobs, warmup=3):
     small = [(p0, p0 + max(10_000, (p1 - p0) // 200), n0, n1) for p0, p1, n0, n1 in jobs]
     for _ in range(warmup):                       # warm-up: the same mix at 1/200 of the p-widths
         ctx.batch_sieve(small)
+    # the batch kernel's tile size, measured on the mix at 1/32 of its p-widths
+    tile = ctx.autotune_batch(jobs, scale_down=32)
     # batched leg
     ctx.batch_prepare(jobs, hitcap=cap)
     ctx.reset_stats()
@@ -626,6 +636,7 @@ def batch_compare(ctx, fs, torch, dev, jobs, warmup=3):
     pairs = sum(r["primecount"] * (j[3] - j[2]) for r, j in zip(res, jobs))
     ctx.batch_release()
     # plain leg: 64 sequential searches
+    ctx.set_tuning()
     ctx.reset_stats()
     ctx.set_timing(True)
     torch.cuda.synchronize(dev)
@@ -654,6 +665,9 @@ def batch_compare(ctx, fs, torch, dev, jobs, warmup=3):
                                  "wall_pair_steps_per_s": pairs / wall_p, "launches": int(sp["launches"])},
             "speedup_device": dev_p / dev_b, "speedup_wall": wall_p / wall_b,
             "per_job_bit_exact": bool(same), "warmup": "the same 64 jobs at 1/200 of their p-widths",
+            "tuning": {"batch_tile_candidates": tile["tile"], "sample_batch_ms": tile["ms"],
+                       "by": "fs_autotune_batch on the mix at 1/32 of its p-widths; the plain leg runs default "
+                             "shapes"},
             "clocks": clk.summary()}
 
 

@@ -67,7 +67,14 @@ class JobResult(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [("sieve_blocks_per_sm", C.c_uint32), ("gen_blocks_per_sm", C.c_uint32),
                 ("max_steps_per_launch", C.c_uint32), ("setup_chunks", C.c_uint32),
-                ("sieve_variant", C.c_uint32)]
+                ("sieve_variant", C.c_uint32), ("sieve_block_threads", C.c_uint32),
+                ("batch_tile_candidates", C.c_uint32)]
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("tuning", Tuning), ("seg_width", C.c_uint64), ("seg_capacity", C.c_uint64),
+                ("setup_words", C.c_uint32), ("steps_per_launch", C.c_uint32), ("rate", C.c_double),
+                ("shapes_tried", C.c_uint32), ("from_cache", C.c_uint32)]
 
 
 _lock = threading.Lock()
@@ -112,6 +119,8 @@ def _declare(L):
         "fs_batch_launch": (C.c_int, [vp]),
         "fs_batch_collect": (C.c_int, [vp, C.POINTER(JobResult), C.POINTER(Factor), u64, P64]),
         "fs_batch_release": (C.c_int, [vp]),
+        "fs_autotune": (C.c_int, [vp, u64, u64, u32, u32, C.c_double, C.c_char_p, C.POINTER(TuneResult)]),
+        "fs_autotune_batch": (C.c_int, [vp, C.POINTER(Job), u32, u32, C.c_char_p, P32, C.POINTER(C.c_double)]),
         "fs_power_table": (C.c_int, [u32, P64, P32, P32, u32, P32]),
         "fs_setup_plan": (C.c_int, [u32, u32, P64, u64, P64, P32, u32, P32, P64]),
         "fs_setup_plan_chunks": (C.c_int, [u32, u32, P32, P64]),
@@ -317,8 +326,9 @@ class Context:
         self._chk(lib().fs_set_stream(self._h, C.c_void_p(stream or 0)), "fs_set_stream")
 
     def set_tuning(self, sieve_blocks_per_sm=0, gen_blocks_per_sm=0, max_steps_per_launch=0,
-                   setup_chunks=0, sieve_variant=0) -> None:
-        t = Tuning(sieve_blocks_per_sm, gen_blocks_per_sm, max_steps_per_launch, setup_chunks, sieve_variant)
+                   setup_chunks=0, sieve_variant=0, sieve_block_threads=0, batch_tile_candidates=0) -> None:
+        t = Tuning(sieve_blocks_per_sm, gen_blocks_per_sm, max_steps_per_launch, setup_chunks, sieve_variant,
+                   sieve_block_threads, batch_tile_candidates)
         self._chk(lib().fs_set_tuning(self._h, C.byref(t)), "fs_set_tuning")
 
     def tuning(self) -> dict:
@@ -434,6 +444,27 @@ class Context:
             out.append(SieveResult(kept, (r["raw_sum"] + cs_add) & 0xFFFFFFFFFFFFFFFF, r["primecount"], len(kept),
                                    r["raw_sum"], len(mine), disc))
         return out
+
+    # measured launch sizing (fs_autotune / fs_autotune_batch)
+    def autotune(self, pmin, pmax, nmin, nmax, target_ms=1000.0, cache_path=None) -> dict:
+        """Time launch shapes on a sample of this search, apply the fastest to the
+        context, and return it with the segment width for target_ms of kernel time."""
+        r = TuneResult()
+        path = cache_path.encode() if cache_path else None
+        self._chk(lib().fs_autotune(self._h, pmin, pmax, nmin, nmax, target_ms, path, C.byref(r)), "fs_autotune")
+        out = {k: getattr(r, k) for k, _ in TuneResult._fields_ if k != "tuning"}
+        out["tuning"] = {k: getattr(r.tuning, k) for k, _ in Tuning._fields_}
+        return out
+
+    def autotune_batch(self, jobs, scale_down=16, cache_path=None) -> dict:
+        """Time the batch kernel's tile sizes on the job mix (p-ranges narrowed
+        scale_down times) and apply the fastest; returns {tile, ms}."""
+        arr = (Job * len(jobs))(*[Job(*map(int, j)) for j in jobs])
+        tile, ms = C.c_uint32(0), C.c_double(0)
+        path = cache_path.encode() if cache_path else None
+        self._chk(lib().fs_autotune_batch(self._h, arr, len(jobs), scale_down, path, C.byref(tile), C.byref(ms)),
+                  "fs_autotune_batch")
+        return {"tile": tile.value, "ms": ms.value}
 
     def plan_check(self, d_cand, d_ctr, nmin, d_words, d_layers4, nlayers, deficit):
         out = np.zeros(2, np.uint64)

@@ -27,7 +27,7 @@ INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["fs_kernels.cu", "fs_sieve2.cu", "fs_sieve4.cu", "fs_multi.cu", "fs_capi.cu", "fs_noalloc.cu",
-              "fs_serve.cu"]
+              "fs_serve.cu", "fs_tune.cu"]
 CXX_SOURCES = ["fs_host.cpp", "fs_post.cpp", "fs_putil.cpp"]
 CLI_SOURCES = ["factsieve_main.cpp", "search.cpp"]
 

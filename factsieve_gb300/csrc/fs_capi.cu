@@ -171,10 +171,16 @@ int variant(fs_ctx* c) { return c->tuning.sieve_variant == 3 ? 3 : 5; }
 // launch-wide walks only; a mixed segment (WALK_ANY) runs variant 3.
 int kernel_variant(int v, int walk) { return (v == 5 && walk == fs::WALK_ANY) ? 3 : v; }
 
-// Default blocks per SM for a build: its resident occupancy, and for the
-// four-candidate build four times that, so the candidates are dealt in
-// smaller shares and the last wave is short.
-int default_bpsm(fs_ctx* c, int kv) { return c->sieve_occ[kv] * (kv == 5 ? 4 : 1); }
+// Threads per sieve block (fs_tuning.sieve_block_threads): 256 or 128.
+int block_threads(fs_ctx* c) { return c->tuning.sieve_block_threads == 128 ? 128 : 256; }
+
+// Default blocks per SM for a build: its resident occupancy at the block
+// size, and for the four-candidate build four times that, so the candidates
+// are dealt in smaller shares and the last wave is short.
+int default_bpsm(fs_ctx* c, int kv) {
+    const int occ = block_threads(c) == 128 ? c->sieve_occ128[kv] : c->sieve_occ[kv];
+    return occ * (kv == 5 ? 4 : 1);
+}
 
 // The build for launches that walk each candidate with its own step.
 int any_variant(fs_ctx* c) { return kernel_variant(variant(c), fs::WALK_ANY); }
@@ -334,7 +340,7 @@ int run_sieve(fs_ctx* c, const u64* d_cand, uint32_t cap, fs::Counters* d_ctr, u
         if (smode == fs::SETUP_PLAN && kv == 5 && (walk == fs::WALK_C96H || walk == fs::WALK_C96) &&
             fs::pm_setup_for_range(plo, phi))
             smode = fs::SETUP_PLAN_PM;
-        CK(c, fs::launch_sieve(a, smode, fin, sieve_grid(c, kv), c->stream, kv, walk));
+        CK(c, fs::launch_sieve(a, smode, fin, sieve_grid(c, kv), c->stream, kv, walk, block_threads(c)));
         if ((rc = ev_end(c, ev, c->sieve_ev))) return rc;
         ++c->launches;
         ++c->sieve_launches;
@@ -414,6 +420,8 @@ int fs_create(int device, fs_ctx** out) {
     for (int v : {3, 5}) {
         int occ = 0;
         if (fs::sieve_occupancy(&occ, v) == cudaSuccess && occ > 0) c->sieve_occ[v] = occ;
+        occ = 0;
+        if (fs::sieve_occupancy(&occ, v, 128) == cudaSuccess && occ > 0) c->sieve_occ128[v] = occ;
     }
     if (cudaMalloc((void**)&c->d_ctr, sizeof(fs::Counters)) != cudaSuccess ||
         cudaMalloc((void**)&c->d_sink, 4096 * sizeof(u32)) != cudaSuccess) {
@@ -494,6 +502,13 @@ void* fs_get_stream(fs_ctx* c) { return c ? (void*)c->stream : nullptr; }
 
 int fs_set_tuning(fs_ctx* c, const fs_tuning* t) {
     if (!c || !t) return FS_E_ARG;
+    if ((t->sieve_variant && t->sieve_variant != 3 && t->sieve_variant != 5) ||
+        (t->sieve_block_threads && t->sieve_block_threads != 128 && t->sieve_block_threads != 256) ||
+        (t->batch_tile_candidates && t->batch_tile_candidates != 1024 && t->batch_tile_candidates != 2048 &&
+         t->batch_tile_candidates != 4096)) {
+        c->err = "unsupported tuning value";
+        return FS_E_ARG;
+    }
     c->tuning = *t;
     return FS_OK;
 }
@@ -503,6 +518,8 @@ int fs_get_tuning(fs_ctx* c, fs_tuning* t) {
     *t = c->tuning;
     if (!t->sieve_variant) t->sieve_variant = (uint32_t)variant(c);
     if (!t->sieve_blocks_per_sm) t->sieve_blocks_per_sm = (uint32_t)default_bpsm(c, variant(c));
+    if (!t->sieve_block_threads) t->sieve_block_threads = (uint32_t)block_threads(c);
+    if (!t->batch_tile_candidates) t->batch_tile_candidates = fs::kTileCandidates;
     return FS_OK;
 }
 
@@ -672,7 +689,8 @@ int fs_setup(fs_ctx* c, const uint64_t* d_cand, uint32_t cap, fs_counters* d_ctr
         CK(c, fs::launch_setup_partial(a, std::max(1, sieve_grid(c, any_variant(c)) / (int)chunks), (int)chunks, c->stream));
         mode = fs::SETUP_PARTIALS;
     }
-    CK(c, fs::launch_sieve(a, mode, false, sieve_grid(c, any_variant(c)), c->stream, any_variant(c), fs::WALK_ANY));
+    CK(c, fs::launch_sieve(a, mode, false, sieve_grid(c, any_variant(c)), c->stream, any_variant(c), fs::WALK_ANY,
+                           block_threads(c)));
     return FS_OK;
 }
 
@@ -697,7 +715,8 @@ int fs_iterate(fs_ctx* c, const uint64_t* d_cand, uint32_t cap, fs_counters* d_c
         uint32_t e = (maxs && nend - s > maxs) ? s + maxs : nend;
         a.nstart = s;
         a.nend = e;
-        CK(c, fs::launch_sieve(a, fs::SETUP_LOAD, false, sieve_grid(c, any_variant(c)), c->stream, any_variant(c), fs::WALK_ANY));
+        CK(c, fs::launch_sieve(a, fs::SETUP_LOAD, false, sieve_grid(c, any_variant(c)), c->stream, any_variant(c),
+                               fs::WALK_ANY, block_threads(c)));
         s = e;
     } while (s < nend);
     return FS_OK;
@@ -718,7 +737,8 @@ int fs_check(fs_ctx* c, const uint64_t* d_cand, uint32_t cap, fs_counters* d_ctr
     a.nstart = a.nend = nmax;
     a.nmax = nmax;
     a.count_candidates = 1;
-    CK(c, fs::launch_sieve(a, fs::SETUP_LOAD, true, sieve_grid(c, any_variant(c)), c->stream, any_variant(c), fs::WALK_ANY));
+    CK(c, fs::launch_sieve(a, fs::SETUP_LOAD, true, sieve_grid(c, any_variant(c)), c->stream, any_variant(c),
+                           fs::WALK_ANY, block_threads(c)));
     return FS_OK;
 }
 
@@ -984,6 +1004,8 @@ extern "C" int fs_batch_prepare(fs_ctx* c, const fs_job* jobs, uint32_t njobs, u
     a.layers = b.d_layers;
     a.hits = b.d_hits;
     a.hitcap = hitcap;
+    // tile size from the context's tuning (fs_autotune_batch measures it)
+    a.tile_candidates = c->tuning.batch_tile_candidates ? c->tuning.batch_tile_candidates : fs::kTileCandidates;
     if (e == cudaSuccess && grc == FS_OK) e = fs::launch_batch(a, c->sm_count * occ, c->stream);
     cudaGraph_t g = nullptr;
     cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);

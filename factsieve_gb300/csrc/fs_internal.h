@@ -33,7 +33,8 @@ struct fs_ctx {
     cudaStream_t own = nullptr, stream = nullptr;
     int sm_count = 0, clock_khz = 0;
     uint64_t total_mem = 0;
-    int sieve_occ[7] = {1, 1, 1, 1, 1, 1, 1};
+    int sieve_occ[7] = {1, 1, 1, 1, 1, 1, 1};      // resident 256-thread sieve blocks per SM, by build
+    int sieve_occ128[7] = {2, 2, 2, 2, 2, 2, 2};   // and 128-thread ones
     fs_tuning tuning{};
     std::string err;
     // search state

@@ -487,13 +487,13 @@ int gen_threads() { return kGenWarps * 32; }
 // thread at 2 blocks per SM, for a step valid over the whole launch (a
 // WALK_ANY launch runs variant 3).
 cudaError_t launch_sieve(const SieveArgs& a, int setup, bool final_chunk, int grid, cudaStream_t s,
-                         int variant, int walk) {
-    if (variant == 5 && walk != WALK_ANY) return launch_sieve_quad(a, setup, final_chunk, grid, s, walk);
-    return launch_sieve_pair(a, setup, final_chunk, grid, s, walk);
+                         int variant, int walk, int threads) {
+    if (variant == 5 && walk != WALK_ANY) return launch_sieve_quad(a, setup, final_chunk, grid, s, walk, threads);
+    return launch_sieve_pair(a, setup, final_chunk, grid, s, walk, threads);
 }
 
-cudaError_t sieve_occupancy(int* blocks_per_sm, int variant) {
-    return variant == 5 ? sieve_quad_occupancy(blocks_per_sm) : sieve_pair_occupancy(blocks_per_sm);
+cudaError_t sieve_occupancy(int* blocks_per_sm, int variant, int threads) {
+    return variant == 5 ? sieve_quad_occupancy(blocks_per_sm, threads) : sieve_pair_occupancy(blocks_per_sm, threads);
 }
 
 }  // namespace fs

@@ -85,6 +85,7 @@ struct BatchArgs {
     const Layer* layers;
     Factor* hits;                // pad = job index
     u32 hitcap;
+    u32 tile_candidates;         // candidates per tile: a multiple of kTileCandidates
 };
 
 // Candidates per tile of the batch and serving kernels (four per thread).
@@ -128,12 +129,16 @@ cudaError_t launch_gen(const GenArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_batch(const BatchArgs& a, int grid, cudaStream_t s);
 cudaError_t batch_occupancy(int* blocks_per_sm);
 int batch_max_jobs();
+// The fused sieve kernel: variant 3 (two candidates per thread) or 5 (four), the walk
+// step, and blocks of `threads` = 256 or 128 threads.
 cudaError_t launch_sieve(const SieveArgs& a, int setup, bool final_chunk, int grid, cudaStream_t s, int variant,
-                         int walk);
-cudaError_t launch_sieve_pair(const SieveArgs& a, int setup, bool final_chunk, int grid, cudaStream_t s, int walk);
-cudaError_t launch_sieve_quad(const SieveArgs& a, int setup, bool final_chunk, int grid, cudaStream_t s, int walk);
-cudaError_t sieve_pair_occupancy(int* blocks_per_sm);
-cudaError_t sieve_quad_occupancy(int* blocks_per_sm);
+                         int walk, int threads = 256);
+cudaError_t launch_sieve_pair(const SieveArgs& a, int setup, bool final_chunk, int grid, cudaStream_t s, int walk,
+                              int threads);
+cudaError_t launch_sieve_quad(const SieveArgs& a, int setup, bool final_chunk, int grid, cudaStream_t s, int walk,
+                              int threads);
+cudaError_t sieve_pair_occupancy(int* blocks_per_sm, int threads);
+cudaError_t sieve_quad_occupancy(int* blocks_per_sm, int threads);
 // The walk step valid for every p in [plo, phi) with multipliers up to kmax.
 int walk_for_range(uint64_t plo, uint64_t phi, uint32_t kmax);
 // 1 when every odd p in [plo, phi) has the form 2^63 + d with 0 < d < 2^30
@@ -143,7 +148,7 @@ cudaError_t launch_setup_partial(const SieveArgs& a, int grid_x, int nchunks, cu
 cudaError_t launch_table_check(const TableCheckArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_imad_bench(u32 iters, u32 kind, u32 seed, u32* sink, int grid, cudaStream_t s);
 double bench_units_per_thread_iter(u32 kind);
-cudaError_t sieve_occupancy(int* blocks_per_sm, int variant);
+cudaError_t sieve_occupancy(int* blocks_per_sm, int variant, int threads = 256);
 int sieve_threads();
 int gen_threads();
 

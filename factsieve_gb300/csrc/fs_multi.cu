@@ -21,7 +21,7 @@ __global__ void __launch_bounds__(kSieveThreads, 2) batch_sieve_kernel(BatchArgs
     __shared__ u32 s_tile;
     __shared__ u64 wsum[kSieveThreads / 32];
     __shared__ u32 wbad[kSieveThreads / 32];
-    const u32 per_tile = kTileCandidates;
+    const u32 per_tile = a.tile_candidates;   // a multiple of kTileCandidates: walked in passes of four per thread
     if (threadIdx.x == 0) {
         st.n = 0;
         u32 acc = 0;
@@ -51,10 +51,12 @@ __global__ void __launch_bounds__(kSieveThreads, 2) batch_sieve_kernel(BatchArgs
         const BatchJob& J = a.jobs[j];
         const u32 nc = a.ctr[j].ncand;
         const u32 n = nc < J.cap ? nc : J.cap;
-        const u32 i0 = (t - (j ? tile_end[j - 1] : 0)) * per_tile + 4 * threadIdx.x;
+        const u32 first = (t - (j ? tile_end[j - 1] : 0)) * per_tile;
         u64 sum = 0;
         u32 bad = 0;
-        if (i0 < n) {
+        for (u32 pass = 0; pass < per_tile; pass += kTileCandidates) {
+            const u32 i0 = first + pass + 4 * threadIdx.x;
+            if (i0 >= n) break;
             const WalkOut o{&st, a.hits, a.hitcap, a.gctr, (int)j};
             Prime c[4];
             const u32 nreal = load_quad(J.cand, i0, n, c);
@@ -247,7 +249,9 @@ __global__ void __launch_bounds__(kSieveThreads, PPT == 4 ? 2 : 3) serve_round_k
 // ============================================================== launches ===
 
 cudaError_t launch_batch(const BatchArgs& a, int grid, cudaStream_t s) {
-    if (a.njobs == 0 || a.njobs > (u32)kBatchMaxJobs) return cudaErrorInvalidValue;
+    if (a.njobs == 0 || a.njobs > (u32)kBatchMaxJobs || a.tile_candidates == 0 ||
+        a.tile_candidates % kTileCandidates)
+        return cudaErrorInvalidValue;
     batch_sieve_kernel<<<grid, kSieveThreads, 0, s>>>(a);
     return cudaGetLastError();
 }

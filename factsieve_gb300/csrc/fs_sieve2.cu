@@ -5,8 +5,7 @@
 namespace fs {
 
 template <int MINB, int WALK, int PPT = 2>
-static void launch_sieve_w(const SieveArgs& a, int setup, bool fin, int grid, cudaStream_t s) {
-    const int t = kSieveThreads;
+static void launch_sieve_w(const SieveArgs& a, int setup, bool fin, int grid, cudaStream_t s, int t) {
     if (setup == SETUP_PLAN || setup == SETUP_PLAN_PM) {   // the pair kernels take every plan with Montgomery products
         if (fin) sieve_kernel<SETUP_PLAN, true, MINB, WALK, PPT><<<grid, t, 0, s>>>(a);
         else sieve_kernel<SETUP_PLAN, false, MINB, WALK, PPT><<<grid, t, 0, s>>>(a);
@@ -19,25 +18,27 @@ static void launch_sieve_w(const SieveArgs& a, int setup, bool fin, int grid, cu
     }
 }
 
-cudaError_t launch_sieve_pair(const SieveArgs& a, int setup, bool final_chunk, int grid, cudaStream_t s, int walk) {
+cudaError_t launch_sieve_pair(const SieveArgs& a, int setup, bool final_chunk, int grid, cudaStream_t s, int walk,
+                              int threads) {
+    if (threads != kSieveThreads && threads != kSieveThreads / 2) return cudaErrorInvalidValue;
     switch (walk) {
-        case WALK_HF: launch_sieve_w<3, WALK_HF>(a, setup, final_chunk, grid, s); break;
-        case WALK_H64: launch_sieve_w<3, WALK_H64>(a, setup, final_chunk, grid, s); break;
-        case WALK_H96: launch_sieve_w<3, WALK_H96>(a, setup, final_chunk, grid, s); break;
-        case WALK_H32: launch_sieve_w<3, WALK_H32>(a, setup, final_chunk, grid, s); break;
-        case WALK_HM: launch_sieve_w<3, WALK_HM>(a, setup, final_chunk, grid, s); break;
-        case WALK_C96H: launch_sieve_w<3, WALK_C96H>(a, setup, final_chunk, grid, s); break;
-        case WALK_T64: launch_sieve_w<3, WALK_T64>(a, setup, final_chunk, grid, s); break;
-        case WALK_L96: launch_sieve_w<3, WALK_L96>(a, setup, final_chunk, grid, s); break;
-        case WALK_C96: launch_sieve_w<3, WALK_C96>(a, setup, final_chunk, grid, s); break;
-        default: launch_sieve_w<3, WALK_ANY>(a, setup, final_chunk, grid, s); break;
+        case WALK_HF: launch_sieve_w<3, WALK_HF>(a, setup, final_chunk, grid, s, threads); break;
+        case WALK_H64: launch_sieve_w<3, WALK_H64>(a, setup, final_chunk, grid, s, threads); break;
+        case WALK_H96: launch_sieve_w<3, WALK_H96>(a, setup, final_chunk, grid, s, threads); break;
+        case WALK_H32: launch_sieve_w<3, WALK_H32>(a, setup, final_chunk, grid, s, threads); break;
+        case WALK_HM: launch_sieve_w<3, WALK_HM>(a, setup, final_chunk, grid, s, threads); break;
+        case WALK_C96H: launch_sieve_w<3, WALK_C96H>(a, setup, final_chunk, grid, s, threads); break;
+        case WALK_T64: launch_sieve_w<3, WALK_T64>(a, setup, final_chunk, grid, s, threads); break;
+        case WALK_L96: launch_sieve_w<3, WALK_L96>(a, setup, final_chunk, grid, s, threads); break;
+        case WALK_C96: launch_sieve_w<3, WALK_C96>(a, setup, final_chunk, grid, s, threads); break;
+        default: launch_sieve_w<3, WALK_ANY>(a, setup, final_chunk, grid, s, threads); break;
     }
     return cudaGetLastError();
 }
 
-cudaError_t sieve_pair_occupancy(int* blocks_per_sm) {
+cudaError_t sieve_pair_occupancy(int* blocks_per_sm, int threads) {
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, sieve_kernel<SETUP_PLAN, true, 3, WALK_ANY, 2>,
-                                                         kSieveThreads, 0);
+                                                         threads, 0);
 }
 
 }  // namespace fs

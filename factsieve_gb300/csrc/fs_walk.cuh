@@ -762,7 +762,7 @@ __global__ void __launch_bounds__(kSieveThreads, MINB) sieve_kernel(SieveArgs a)
     if (FINAL && threadIdx.x == 0) {
         u64 s = 0;
         u32 b = 0;
-        for (int w = 0; w < kSieveThreads / 32; ++w) {
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {   // blocks of 256 or 128 threads
             s += wsum[w];
             b += wbad[w];
         }

@@ -162,19 +162,6 @@ int setup_search(WorkStatus& st, SearchOptions& so) {
     return 0;
 }
 
-// p-width of a segment: about 2e11 (p,n) steps of GPU work, or the whole range.
-uint64_t segment_width(const WorkStatus& st, const SearchOptions& so) {
-    if (so.seg_width) return so.seg_width;
-    // about 1.5e12 (p,n) steps per segment (under a second on a GB300): long
-    // enough that the last partial wave of a launch costs little, short
-    // enough for a progress line every second or so
-    const double lp = std::log(std::max<double>((double)st.p, 3.0));
-    const double per_cand = (double)(st.nmax - st.nmin) + 0.036 * st.nmin + 64.0;
-    double w = 1.5e12 * lp / per_cand;
-    w = std::min(std::max(w, 1e5), 4e9);
-    return (uint64_t)w;
-}
-
 bool factor_less(const fs_factor& a, const fs_factor& b) {
     if (a.p != b.p) return a.p < b.p;
     const int32_t na = a.nc < 0 ? -a.nc : a.nc, nb = b.nc < 0 ? -b.nc : b.nc;
@@ -351,17 +338,29 @@ int run_search(WorkStatus& st, SearchOptions& so) {
         ~Closer() { fs_destroy(c); }
     } closer{ctx};
 
-    if ((rc = fs_search_begin(ctx, st.pmin, st.pmax, st.nmin, st.nmax, so.numresults))) {
-        both("error: %s %s\n", fs_strerror(rc), fs_last_error(ctx));
-        return EXIT_FAILURE;
-    }
     std::vector<fs_factor> buf(so.numresults);
     int sms = 0, clk = 0;
     uint64_t mem = 0;
     fs_device_info(ctx, &sms, &clk, &mem);
-    const uint64_t width = segment_width(st, so);
-    both("c:1 u:%d t:%u r:%" PRIu64 "\n", sms, so.threads, width);
+    // measured launch sizing (profileGPU and the setup/iterate retuning,
+    // cl_sieve.cpp:617-718, 1158-1227), on what is left of the range
+    fs_tune_result tr{};
+    if ((rc = fs_autotune(ctx, st.p, st.pmax, st.nmin, st.nmax, so.segment_ms, getenv("FS_TUNING_CACHE"), &tr))) {
+        both("error: %s %s\n", fs_strerror(rc), fs_last_error(ctx));
+        return EXIT_FAILURE;
+    }
+    const uint64_t width = so.seg_width ? so.seg_width : tr.seg_width;
+    both("c:1 u:%d t:%u r:%" PRIu64 " p:%" PRIu64 " s:%u n:%u\n", sms, so.threads, width,
+         fs_candidate_capacity(st.p, st.p + width), tr.setup_words, tr.steps_per_launch);
+    say("launch shape: %u candidates per thread, %u blocks of %u threads per SM%s, %.3g (p,n) steps/s measured%s\n",
+        tr.tuning.sieve_variant == 5 ? 4u : 2u, tr.tuning.sieve_blocks_per_sm, tr.tuning.sieve_block_threads,
+        tr.tuning.max_steps_per_launch ? ", n-range split" : "", tr.rate,
+        tr.from_cache ? " (cached)" : (tr.shapes_tried ? "" : " (run too small to time: defaults)"));
 
+    if ((rc = fs_search_begin(ctx, st.pmin, st.pmax, st.nmin, st.nmax, so.numresults))) {
+        both("error: %s %s\n", fs_strerror(rc), fs_last_error(ctx));
+        return EXIT_FAILURE;
+    }
     const time_t t_start = time(nullptr);
     time_t t_progress = t_start, t_ckpt = t_start;
     const double irsize = 1.0 / (double)(st.pmax - st.pmin ? st.pmax - st.pmin : 1);

@@ -15,7 +15,8 @@ struct SearchOptions {
     bool test = false;               // -s: self test
     int device = 0;                  // CUDA device
     uint32_t numresults = 1000000;   // factor buffer (main.cpp:193, cl_sieve.cpp:593-595)
-    uint64_t seg_width = 0;          // p-width of a GPU segment (0: automatic)
+    uint64_t seg_width = 0;          // p-width of a GPU segment (0: measured, about segment_ms of kernel time)
+    double segment_ms = 2000;        // kernel time a measured segment aims at
     double checkpoint_seconds = 60;  // time between checkpoints (cl_sieve.cpp:1125)
     bool write_state_a_next = true;  // A/B alternation of the checkpoint files
 };

@@ -74,6 +74,8 @@ typedef struct {
     uint32_t sieve_variant;         /* sieve kernel build: 3 = two candidates per thread at 3 resident blocks per
                                        SM; 5 (default) = four candidates per thread at 2 (segments whose
                                        candidates share one walk step; a mixed segment runs build 3) */
+    uint32_t sieve_block_threads;   /* threads per sieve block: 256 (default) or 128 */
+    uint32_t batch_tile_candidates; /* candidates per tile of the batch kernel: 1024 (default), 2048 or 4096 */
 } fs_tuning;
 
 /* ---- library / device ---------------------------------------------------- */
@@ -152,6 +154,42 @@ int fs_batch_launch(fs_ctx *ctx);
 int fs_batch_collect(fs_ctx *ctx, fs_job_result *results, fs_factor *hits, uint64_t hitcap, uint64_t *nhits);
 /* Free the batch's device memory and graph. */
 int fs_batch_release(fs_ctx *ctx);
+
+/* ---- measured launch sizing (cl_sieve.cpp:617-718, 1158-1227) -------------- */
+/* The reference times one generator launch and scales a segment's p-range to
+ * 1 ms of it (profileGPU), then times one setup and one iterate launch and
+ * scales their work to 10-50 ms; it prints the result as
+ * "c:%u u:%u t:%u r:%u p:%u s:%u n:%u".  fs_autotune times whole segment
+ * searches of a sample of the real workload (its first p-values, the real
+ * n-range) for each launch shape -- candidates per thread (sieve_variant 3 or
+ * 5), blocks per SM (1x, 2x, 4x the resident ones), threads per block (256 or
+ * 128), n-steps per launch (all, or halves) -- applies the fastest to the
+ * context and sizes a segment to about target_ms (<= 0: 1000) of kernel time
+ * at the measured rate.  The choice is cached in the text file cache_path
+ * (NULL: no cache) under the GPU name, SM count and the workload's bucket
+ * (log2 of the n-width, of p and of nmin); a cached choice is applied without
+ * timing.  Runs its own sample searches on the context: call it before
+ * fs_search_begin.  Results never depend on the shape. */
+typedef struct {
+    fs_tuning tuning;            /* the shape chosen, now the context's (fs_get_tuning form) */
+    uint64_t seg_width;          /* p-width of one segment (the reference's range, r:) */
+    uint64_t seg_capacity;       /* candidate slots such a segment reserves (psize, p:) */
+    uint32_t setup_words;        /* setup-plan words one launch multiplies per candidate (sstep, s:) */
+    uint32_t steps_per_launch;   /* n-steps one launch walks (nstep, n:) */
+    double rate;                 /* (p,n) steps/s of the chosen shape on the sample; 0 when not timed */
+    uint32_t shapes_tried;       /* shapes timed (0: from the cache, or a run too small to sample) */
+    uint32_t from_cache;         /* 1 when the choice came from cache_path */
+} fs_tune_result;
+int fs_autotune(fs_ctx *ctx, uint64_t pmin, uint64_t pmax, uint32_t nmin, uint32_t nmax, double target_ms,
+                const char *cache_path, fs_tune_result *out);
+/* The tile size of the batch kernel (fs_tuning.batch_tile_candidates: 1024,
+ * 2048 or 4096 candidates) for a job mix: each size is timed on the mix with
+ * every p-range narrowed scale_down times (0: 16), the fastest is applied to
+ * the context and cached under the GPU and a hash of the job list.  Call it
+ * before fs_batch_prepare; it releases any prepared batch.  *tile_out gets the
+ * size, *ms_out the timed batch-kernel milliseconds (0 from the cache). */
+int fs_autotune_batch(fs_ctx *ctx, const fs_job *jobs, uint32_t njobs, uint32_t scale_down, const char *cache_path,
+                      uint32_t *tile_out, double *ms_out);
 
 /* ---- serving: continuous batching of search requests ----------------------- */
 /* No counterpart in the reference.  Requests queue on the host; each

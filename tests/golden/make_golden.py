@@ -2,6 +2,7 @@
 
     python tests/golden/make_golden.py [case ...]      (default: the quick cases)
     python tests/golden/make_golden.py --all            (adds the long ones)
+    python tests/golden/make_golden.py config4_slices   (the 64-job mix on 1/1000 p-slices)
 
 Each case writes tests/golden/run_<name>.json with the reference-visible
 result of the whole search (primecount, checksum, factorcount), the raw
@@ -99,6 +100,30 @@ def run_case(name):
           f"checksum {rec['checksum']} ({dt:.1f} s)", flush=True)
 
 
+def write_config4_slices(div=1000):
+    """The 64-job mix (jobs_config4.json, seed 1), each job's p-range cut to its
+    first 1/div (at least 2000 wide), searched job by job with the oracle:
+    run_config4_slices.json holds each sliced job and its result."""
+    with open(os.path.join(HERE, "jobs_config4.json")) as fh:
+        jobs = [tuple(j) for j in json.load(fh)["jobs"]]
+    out = []
+    t0 = time.time()
+    for p0, p1, n0, n1 in jobs:
+        w = max((p1 - p0) // div, 2000)
+        r = oracle.run(p0, p0 + w, n0, n1, seg_width=10_000_000)
+        assert r["status"] == 0 and r["nvalidfail"] == 0
+        out.append({"pmin": p0, "pmax": p0 + w, "nmin": n0, "nmax": n1, "primecount": r["primecount"],
+                    "raw_sum": f"{r['raw_sum']:016X}", "checksum": f"{r['checksum']:016X}",
+                    "factorcount": r["factorcount"], "nhits": r["nhits"], "factors": factor_lines(r["factors"])})
+    dt = time.time() - t0
+    with open(os.path.join(HERE, "run_config4_slices.json"), "w") as fh:
+        json.dump({"name": "config4_slices", "slice": f"first 1/{div} of each job's p-range (>= 2000 wide)",
+                   "oracle_seconds": round(dt, 1), "oracle_threads": oracle.max_threads(), "jobs": out}, fh,
+                  indent=1)
+    print(f"run_config4_slices.json: {len(out)} jobs, {sum(j['primecount'] for j in out)} candidates "
+          f"({dt:.1f} s)", flush=True)
+
+
 def write_candidates():
     ranges = [
         (127, 20_000), (1_000_000, 1_030_000), ((1 << 32) - 20_000, (1 << 32) + 20_000),
@@ -125,5 +150,8 @@ if __name__ == "__main__":
         names = QUICK
     if not args or "--all" in args:
         write_candidates()
+    if "config4_slices" in names or "--all" in args:
+        write_config4_slices()
     for n in names:
-        run_case(n)
+        if n != "config4_slices":
+            run_case(n)

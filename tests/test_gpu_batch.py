@@ -52,3 +52,55 @@ def test_batch_matches_oracle(ctx, orc):
     for j, g in zip(jobs, got):
         w = orc.run(*j)
         assert (g.primecount, g.checksum, g.factorcount) == (w["primecount"], w["checksum"], w["factorcount"]), j
+
+
+def _config4_slices():
+    import json
+    import os
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "run_config4_slices.json")
+    with open(path) as fh:
+        return json.load(fh)["jobs"]
+
+
+def test_config4_mix_on_slices_matches_oracle(ctx):
+    """The 64-job mix (seed 1) with each p-range cut to its first 1/1000, as
+    one batch: every job equals the oracle's search of it (the fixture
+    run_config4_slices.json, made by tests/golden/make_golden.py)."""
+    want = _config4_slices()
+    jobs = [(j["pmin"], j["pmax"], j["nmin"], j["nmax"]) for j in want]
+    got = ctx.batch_sieve(jobs, threads=8)
+    for j, g, w in zip(jobs, got, want):
+        assert (g.primecount, g.raw_sum, g.checksum, g.factorcount, g.nhits) == \
+            (w["primecount"], int(w["raw_sum"], 16), int(w["checksum"], 16), w["factorcount"], w["nhits"]), j
+
+
+def test_config4_mix_on_slices_served_matches_oracle(ctx):
+    """The same 64 sliced jobs through the serving loop, submitted in the
+    stream's order while earlier ones are resident."""
+    import factsieve_gb300 as fs
+    from factsieve_gb300.serve import Server
+    want = _config4_slices()
+    srv = Server(ctx, max_active=16, round_budget=3_000_000_000, mem_reserve=1 << 30)
+    done = {}
+    try:
+        for k, j in enumerate(want):
+            srv.submit((j["pmin"], j["pmax"], j["nmin"], j["nmax"]), k)
+            if k % 4 == 3:
+                srv.round()
+                for d in srv.poll():
+                    done[d["id"]] = d
+        rounds = 0
+        while len(done) < len(want):
+            srv.round()
+            rounds += 1
+            for d in srv.poll():
+                done[d["id"]] = d
+            assert rounds < 20000
+    finally:
+        srv.close()
+    for k, w in enumerate(want):
+        d = done[k]
+        kept, cs_add, _ = fs.postprocess(d["hits"], threads=8)
+        assert d["flags"] == 0
+        assert (d["primecount"], d["raw_sum"], (d["raw_sum"] + cs_add) & ((1 << 64) - 1)) == \
+            (w["primecount"], int(w["raw_sum"], 16), int(w["checksum"], 16)), k

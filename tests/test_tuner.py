@@ -1,59 +1,77 @@
-"""Autotuner: candidate generation, bucket cache, and (GPU) that a tuned
-launch shape leaves results unchanged."""
+"""The native tuner (fs_autotune, fs_autotune_batch): it times launch shapes
+on a sample, applies the fastest, caches the choice per GPU and workload
+bucket, and never changes results."""
 import pytest
 
 from factsieve_gb300 import tuner
 
+pytestmark = pytest.mark.gpu
 
-class FakeCtx:
-    sm_count = 152
-
-    def __init__(self):
-        self.t = {}
-
-    def set_tuning(self, **kw):
-        self.t = kw
-
-    def tuning(self):
-        v = self.t.get("sieve_variant", 3)
-        return {"sieve_variant": v, "sieve_blocks_per_sm": {3: 3, 5: 8}[v]}
+SEARCH = (10**12, 10**12 + 30_000_000, 100_000, 101_000)
 
 
-def test_autotune_picks_fastest_and_caches(tmp_path):
-    cache = tuner.TuningCache(str(tmp_path / "t.json"))
-    calls = []
-
-    def timer(ctx, cfg, pmin, width, nmin, nmax):
-        calls.append(cfg)
-        return 100.0 * cfg["sieve_variant"] - cfg["sieve_blocks_per_sm"]   # best: variant 5 at 8 blocks
-
-    ctx = FakeCtx()
-    best = tuner.autotune(ctx, 10**12, 100_000, 200_000, gpu_name="X", cache=cache, timer=timer)
-    assert (best["sieve_variant"], best["sieve_blocks_per_sm"]) == (5, 8)
-    assert len(calls) == 4
-    again = tuner.autotune(ctx, 10**12 + 5, 100_001, 200_003, gpu_name="X", cache=cache, timer=timer)
-    assert len(calls) == 4 and again["sieve_variant"] == 5          # same bucket: cached
-    tuner.autotune(ctx, 10**15, 100_000, 200_000, gpu_name="X", cache=cache, timer=timer)
-    assert len(calls) == 8                                            # new p bucket: tuned again
-
-
-def test_bucket_key_separates_workloads():
-    a = tuner.bucket_key("GB300", 152, 10**12, 10**5, 2 * 10**5)
-    assert a != tuner.bucket_key("GB300", 152, 2**63, 10**6, 10**6 + 10**4)
-    assert a == tuner.bucket_key("GB300", 152, 10**12 + 10**9, 10**5 + 7, 2 * 10**5 + 7)
-
-
-@pytest.mark.gpu
-def test_tuned_shape_gives_identical_results(ctx, tmp_path):
-    import torch
-    cache = tuner.TuningCache(str(tmp_path / "t.json"))
-    best = tuner.autotune(ctx, 10**12, 100_000, 101_000, gpu_name=torch.cuda.get_device_name(0),
-                          sample_steps=2e9, cache=cache)
-    assert best["rate"] > 0 and len(best["tried"]) == 4
-    base = ctx.sieve(10**12, 10**12 + 3_000_000, 100_000, 101_000)
-    tuner.apply(ctx, best)
+def test_tuned_search_gives_identical_results_and_is_cached(ctx, tmp_path):
+    cache = str(tmp_path / "tuning.txt")
+    base = ctx.sieve(*SEARCH)
+    best = tuner.autotune(ctx, *SEARCH, target_ms=500, cache_path=cache)
     try:
-        tuned = ctx.sieve(10**12, 10**12 + 3_000_000, 100_000, 101_000)
+        assert best["shapes_tried"] >= 6 and best["rate"] > 0 and not best["from_cache"]
+        t = best["tuning"]
+        assert t["sieve_variant"] in (3, 5) and t["sieve_block_threads"] in (128, 256)
+        assert ctx.tuning()["sieve_variant"] == t["sieve_variant"]        # applied to the context
+        assert 1e5 <= best["seg_width"] <= 4_294_900_000
+        assert best["steps_per_launch"] in (1000, 500)
+        tuned = ctx.sieve(*SEARCH, seg_width=best["seg_width"])
+        assert (tuned.raw_sum, tuned.primecount, tuned.checksum) == (base.raw_sum, base.primecount, base.checksum)
+        # the same bucket again: read from the cache, nothing timed
+        again = tuner.autotune(ctx, 10**12 + 7, 10**12 + 20_000_000, 100_003, 101_003, cache_path=cache)
+        assert again["from_cache"] == 1 and again["shapes_tried"] == 0
+        assert again["tuning"] == best["tuning"]
+        lines = open(cache).read().splitlines()
+        assert len(lines) == 1 and lines[0].startswith("search|")
     finally:
         ctx.set_tuning()
-    assert (tuned.raw_sum, tuned.primecount, tuned.checksum) == (base.raw_sum, base.primecount, base.checksum)
+
+
+@pytest.mark.parametrize("shape", [
+    dict(sieve_variant=3, sieve_blocks_per_sm=6, sieve_block_threads=128),
+    dict(sieve_variant=5, sieve_blocks_per_sm=16, sieve_block_threads=128),
+    dict(sieve_variant=5, sieve_blocks_per_sm=2, sieve_block_threads=256, max_steps_per_launch=333),
+])
+def test_every_shape_the_tuner_tries_gives_identical_results(ctx, orc, shape):
+    lo, hi, nmin, nmax = 10**12, 10**12 + 3_000_000, 100_000, 101_000
+    want = orc.run(lo, hi, nmin, nmax)
+    ctx.set_tuning(**shape)
+    try:
+        r = ctx.sieve(lo, hi, nmin, nmax)
+    finally:
+        ctx.set_tuning()
+    assert (r.raw_sum, r.primecount, r.checksum) == (want["raw_sum"], want["primecount"], want["checksum"])
+
+
+def test_tuned_batch_tile_gives_identical_results(ctx, tmp_path):
+    jobs = [(10**9 + 7, 10**9 + 4_000_007, 5000, 6000), (10**12, 10**12 + 6_000_000, 100_000, 100_500),
+            ((1 << 40) + 1, (1 << 40) + 2_000_001, 20_000, 22_000)]
+    base = ctx.batch_sieve(jobs)
+    cache = str(tmp_path / "tuning.txt")
+    got = tuner.autotune_batch(ctx, jobs, scale_down=4, cache_path=cache)
+    try:
+        assert got["tile"] in (1024, 2048, 4096) and got["ms"] > 0
+        assert ctx.tuning()["batch_tile_candidates"] == got["tile"]
+        for tile in (1024, 2048, 4096):
+            ctx.set_tuning(batch_tile_candidates=tile)
+            res = ctx.batch_sieve(jobs)
+            assert [(r.raw_sum, r.primecount, r.checksum) for r in res] == \
+                [(r.raw_sum, r.primecount, r.checksum) for r in base]
+        again = tuner.autotune_batch(ctx, jobs, scale_down=4, cache_path=cache)
+        assert again == {"tile": got["tile"], "ms": 0.0}
+    finally:
+        ctx.set_tuning()
+
+
+def test_tuning_values_are_checked(ctx):
+    import factsieve_gb300 as fs
+    for bad in (dict(sieve_block_threads=64), dict(sieve_variant=4), dict(batch_tile_candidates=512)):
+        with pytest.raises(fs.FSError):
+            ctx.set_tuning(**bad)
+    ctx.set_tuning()
