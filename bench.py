@@ -66,10 +66,10 @@ IMAD_PER_PRODUCT = 20   # reference m_mul on 32-bit limbs (8 mul_wide + 4 + 8)
 # busy share, from one `ncu --set full --clock-control none` capture of the
 # fused sieve kernel on the same workload (dram__bytes_read.sum +
 # dram__bytes_write.sum; sm__pipe_fmaheavy_cycles_active): config 2 captured
-# on a 1e8-wide segment (29,120,512 B) and scaled by 10 to the whole-range
+# on a 1e8-wide segment (29,084,928 B) and scaled by 10 to the whole-range
 # launch the bench times, config 3 on one of its 1e8-wide launches.
 NCU_CAPTURE = {
-    "config2": {"traffic": 291_205_120, "imad_pipe_busy": 0.773,
+    "config2": {"traffic": 290_849_280, "imad_pipe_busy": 0.782,
                 "source": "ncu --set full capture of sieve_kernel, bench.py --segment 1e8"},
     "config3": {"traffic": 18_765_568, "imad_pipe_busy": 0.836,
                 "source": "ncu --set full capture of sieve_kernel, bench.py --workload config3"},

@@ -553,29 +553,31 @@ __device__ __forceinline__ u32 half_walk8x2(u32& al, u32& ah, u32& bl, u32& bh, 
 // IMAD.HI on the integer multiply pipe, which bounds the walk.  This step
 // takes it on the FP32 pipe instead and keeps the multiplies that form
 // t = r k and r' = t + q (2^64 - p).  Let s = bitlen(f) - 4 for a floor
-// f <= p with s >= 35, z = floor(t / 2^s) and Mf = 2^s/p rounded down to
-// 24 bits.  The estimate floor(z Mf) comes from three exact instructions,
-// one integer shift and two float operations:
-//   1. A funnel shift of t's high word, with 2^(s-35) shifted in above it,
-//      gives the bit pattern of the float F = 2^-63 + z 2^-86.  Its exponent
-//      field is 64 and its mantissa is z, which needs z < 2^23.
-//   2. F - 2^-63 = z 2^-86 is exact by Sterbenz's lemma.
-//   3. fma rounding down, by Mf 2^-63, gives z Mf 2^-149.  That lies below
-//      2^-126, on the subnormal grid, so its bit pattern is the integer
-//      floor(z Mf).
+// f <= p with s >= 35, z = floor(t / 2^s) and m = floor(2^e / p) with
+// e = bitlen(p) + 23 (so m has 24 bits and m 2^(s-e) is 2^s/p rounded down
+// to 24 bits).  The estimate floor(z m 2^(s-e)) comes from two exact
+// instructions:
+//   1. z = (t's high word) >> (s - 32).  Read as a float, the bit pattern of
+//      an integer z < 2^23 is the subnormal z 2^-149 (exponent field 0).
+//   2. fma rounding down, by the normal float m 2^(s-e), gives
+//      z m 2^(s-e-149).  That lies below 2^-126, on the subnormal grid, so
+//      its bit pattern is the integer floor(z m 2^(s-e)).
+// The two float operations have no .ftz, so subnormal inputs and results are
+// kept.  (An earlier form built the normal float 2^-63 + z 2^-86 with a
+// funnel shift and subtracted 2^-63 exactly; it gives the same estimate with
+// one instruction more per step: 9 % slower on the walk block.)
 // The estimate never exceeds t/p.  It falls short of it by less than
 // 1 + 2^s/p + (t/p) 2^-23, which is below 1 + 1/8 + 1/16 when
 // r < (19/16) p and 19 k_max <= 2^23.  So r stays below (19/16) p < x + p,
 // and the exact test is r in {x, x + 1}, as in the half-offset lazy step.
 // Validity over a launch (checked by the host, walk_for_range), with f the
 // thread's least candidate: p >= 2^38, p k_max <= 2^62, 19 k_max <= 2^23,
-// and 19 p_max k_max < 2^(bitlen(p_min) + 23), which keeps z < 2^23.  The
-// two float instructions have no .ftz, so subnormals are kept.
+// and 19 p_max k_max < 2^(bitlen(p_min) + 23), which keeps z < 2^23.
 struct HalfF {
     u64 p, x;
     u32 np0, np1;             // 2^64 - p
-    float mf;                 // (2^s/p rounded down to 24 bits) 2^-63
-    u32 sh, hc;               // s - 32 and 2^(s - 35): the funnel shift that builds F
+    float g;                  // m 2^(s - e): 2^s/p rounded down to 24 bits
+    u32 sh;                   // s - 32: the shift that takes z from t's high word
     u32 x0, x1;               // low words of x and x + 1
 };
 
@@ -589,31 +591,29 @@ __device__ __forceinline__ HalfF make_halff(const Prime& c, u64 f) {
     H.np0 = (u32)np;
     H.np1 = (u32)(np >> 32);
     const int bl = bitlen64(c.p), s = bitlen64(f) - 4, e = bl + 23;
-    // m = floor(2^e / p) in [2^23, 2^24): 2^s/p rounded down to 24 bits is m 2^(s-e)
+    // m = floor(2^e / p) in [2^23, 2^24)
     const u32 m = e <= 64 ? (u32)(((~0ull) / c.p) >> (64 - e)) : recip_pow2(c.p, e);
-    // m 2^(s - e - 63) as a float: exponent field s - bl + 64 (normal), mantissa m - 2^23
-    H.mf = __uint_as_float(((u32)(s - bl + 63) << 23) + m);
+    // m 2^(s - e) as a float: exponent field s - e + 150 (normal), mantissa m - 2^23
+    H.g = __uint_as_float(((u32)(s - e + 149) << 23) + m);
     H.sh = (u32)(s - 32);
-    H.hc = 1u << (s - 35);
     H.x0 = (u32)H.x;
     H.x1 = (u32)(H.x + 1);
     return H;
 }
 
-// floor(z Mf) from t's high word, as the PTX block computes it.
+// floor(z m 2^(s-e)) from t's high word, as the PTX block computes it.
 __device__ __forceinline__ u32 halff_quot(u32 th, const HalfF& H) {
     u32 q;
     asm("{\n\t"
         ".reg .b32 z;\n\t"
         ".reg .f32 f;\n\t"
-        "shf.r.wrap.b32 z, %1, %2, %3;\n\t"
+        "shr.u32 z, %1, %2;\n\t"
         "mov.b32 f, z;\n\t"
-        "sub.rn.f32 f, f, 0f20000000;\n\t"
-        "fma.rm.f32 f, f, %4, 0f00000000;\n\t"
+        "fma.rm.f32 f, f, %3, 0f00000000;\n\t"
         "mov.b32 %0, f;\n\t"
         "}"
         : "=r"(q)
-        : "r"(th), "r"(H.hc), "r"(H.sh), "f"(H.mf));
+        : "r"(th), "r"(H.sh), "f"(H.g));
     return q;
 }
 
@@ -624,25 +624,24 @@ __device__ __forceinline__ u64 halff_step(u64 r, u32 k, const HalfF& H) {
 }
 __device__ __forceinline__ u64 halff_canon(u64 r, const HalfF& H) { return r >= H.p ? r - H.p : r; }
 
-#define FS_HFF_MUL(RL, RH, NP0, NP1, MF, SH, HC, T, R, TL, TH, Q, Z, F, KK) \
+#define FS_HFF_MUL(RL, RH, NP0, NP1, G, SH, T, TL, TH, Q, Z, F, KK)      \
     "mul.wide.u32 " T ", " RL ", " KK ";\n\t"                                \
     "mov.b64 {" TL ", " TH "}, " T ";\n\t"                                   \
     "mad.lo.u32 " TH ", " RH ", " KK ", " TH ";\n\t"                         \
-    "shf.r.wrap.b32 " Z ", " TH ", " HC ", " SH ";\n\t"                  \
+    "shr.u32 " Z ", " TH ", " SH ";\n\t"                                    \
     "mov.b32 " F ", " Z ";\n\t"                                          \
-    "sub.rn.f32 " F ", " F ", 0f20000000;\n\t"                           \
-    "fma.rm.f32 " F ", " F ", " MF ", 0f00000000;\n\t"                   \
+    "fma.rm.f32 " F ", " F ", " G ", 0f00000000;\n\t"                   \
     "mov.b32 " Q ", " F ";\n\t"                                          \
     "mad.lo.cc.u32 " RL ", " Q ", " NP0 ", " TL ";\n\t"                  \
     "madc.hi.u32 " TH ", " Q ", " NP0 ", " TH ";\n\t"                    \
     "mad.lo.u32 " RH ", " Q ", " NP1 ", " TH ";\n\t"
-// The multipliers k1 .. k1 + 7 come in as operands %20-%27: computed outside
+// The multipliers k1 .. k1 + 7 come in as operands %18-%25: computed outside
 // the asm, they are shared by the blocks of a thread's two pairs.
-#define FS_HFF_STEP2(KK)                                                                             \
-    FS_HF_TEST("%0", "%9", "%10")                                                                    \
-    FS_HF_TEST("%2", "%16", "%17")                                                                   \
-    FS_HFF_MUL("%0", "%1", "%6", "%7", "%8", "%11", "%12", "TA", "RA", "aL", "aH", "qA", "zA", "fA", KK) \
-    FS_HFF_MUL("%2", "%3", "%13", "%14", "%15", "%18", "%19", "TB", "RB", "bL", "bH", "qB", "zB", "fB", KK)
+#define FS_HFF_STEP2(KK)                                                                 \
+    FS_HF_TEST("%0", "%9", "%10")                                                        \
+    FS_HF_TEST("%2", "%15", "%16")                                                       \
+    FS_HFF_MUL("%0", "%1", "%6", "%7", "%8", "%11", "TA", "aL", "aH", "qA", "zA", "fA", KK)   \
+    FS_HFF_MUL("%2", "%3", "%12", "%13", "%14", "%17", "TB", "bL", "bH", "qB", "zB", "fB", KK)
 
 // Eight float-quotient half-offset steps on two residues; the flag as
 // lazy_walk8x2's.
@@ -652,16 +651,16 @@ __device__ __forceinline__ u32 halff_walk8x2(u32& al, u32& ah, u32& bl, u32& bh,
     asm("{\n\t"
         ".reg .u32 aL, aH, qA, zA, bL, bH, qB, zB;\n\t"
         ".reg .f32 fA, fB;\n\t"
-        ".reg .u64 TA, RA, TB, RB;\n\t"
+        ".reg .u64 TA, TB;\n\t"
         ".reg .pred P;\n\t"
         "setp.ne.u32 P, %5, %5;\n\t"
-        FS_HFF_STEP2("%20") FS_HFF_STEP2("%21") FS_HFF_STEP2("%22") FS_HFF_STEP2("%23")
-        FS_HFF_STEP2("%24") FS_HFF_STEP2("%25") FS_HFF_STEP2("%26") FS_HFF_STEP2("%27")
+        FS_HFF_STEP2("%18") FS_HFF_STEP2("%19") FS_HFF_STEP2("%20") FS_HFF_STEP2("%21")
+        FS_HFF_STEP2("%22") FS_HFF_STEP2("%23") FS_HFF_STEP2("%24") FS_HFF_STEP2("%25")
         "selp.u32 %4, 1, 0, P;\n\t"
         "}"
         : "+r"(al), "+r"(ah), "+r"(bl), "+r"(bh), "=r"(flag)
-        : "r"(k1), "r"(A.np0), "r"(A.np1), "f"(A.mf), "r"(A.x0), "r"(A.x1), "r"(A.sh), "r"(A.hc),
-          "r"(B.np0), "r"(B.np1), "f"(B.mf), "r"(B.x0), "r"(B.x1), "r"(B.sh), "r"(B.hc),
+        : "r"(k1), "r"(A.np0), "r"(A.np1), "f"(A.g), "r"(A.x0), "r"(A.x1), "r"(A.sh),
+          "r"(B.np0), "r"(B.np1), "f"(B.g), "r"(B.x0), "r"(B.x1), "r"(B.sh),
           "r"(k1), "r"(k1 + 1), "r"(k1 + 2), "r"(k1 + 3), "r"(k1 + 4), "r"(k1 + 5), "r"(k1 + 6), "r"(k1 + 7));
     return flag;
 }

@@ -213,24 +213,22 @@ def _f32(bits):
 
 def _halff_step(r, k, p, f):
     """Word-level restatement of halff_step (fs_arith.cuh) with exact rationals:
-    funnel shift into the float 2^-63 + z 2^-86, exact subtraction, fma rounding
-    down onto the subnormal grid."""
+    z = (t's high word) >> (s - 32) read as the subnormal z 2^-149, one fma by
+    m 2^(s-e) rounding down onto the subnormal grid."""
     from fractions import Fraction
     bl, s = p.bit_length(), f.bit_length() - 4
     e = bl + 23
     m = (1 << e) // p
-    mf = _f32(((s - bl + 63) << 23) + m)
-    assert mf == Fraction(m, 1 << (e - s + 63))
-    sh, hc = s - 32, 1 << (s - 35)
+    assert (1 << 23) <= m < (1 << 24)
+    g = _f32(((s - e + 149) << 23) + m)
+    assert g == Fraction(m, 1 << (e - s))
     t = r * k
     assert t < 1 << 64
-    th = t >> 32
-    z = th >> sh
+    z = (t >> 32) >> (s - 32)
     assert z < 1 << 23
-    fbits = (z | (hc << (32 - sh))) & 0xFFFFFFFF
-    assert _f32(fbits) == Fraction(1, 1 << 63) + Fraction(z, 1 << 86)
-    prod = (_f32(fbits) - Fraction(1, 1 << 63)) * mf
-    assert prod < Fraction(1, 1 << 126)
+    assert _f32(z) == Fraction(z, 1 << 149)                  # exponent field 0: the subnormal z 2^-149
+    prod = _f32(z) * g
+    assert prod < Fraction(1, 1 << 126)                      # on the subnormal grid
     q = int(prod * (1 << 149))
     return (t + q * ((1 << 64) - p)) % (1 << 64)
 
