@@ -68,11 +68,17 @@ IMAD_PER_PRODUCT = 20   # reference m_mul on 32-bit limbs (8 mul_wide + 4 + 8)
 # dram__bytes_write.sum; sm__pipe_fmaheavy_cycles_active): config 2 captured
 # on a 1e8-wide segment (29,084,928 B) and scaled by 10 to the whole-range
 # launch the bench times, config 3 on one of its 1e8-wide launches.
-NCU_CAPTURE = {
-    "config2": {"traffic": 290_849_280, "imad_pipe_busy": 0.782,
-                "source": "ncu --set full capture of sieve_kernel, bench.py --segment 1e8"},
-    "config3": {"traffic": 18_765_568, "imad_pipe_busy": 0.836,
-                "source": "ncu --set full capture of sieve_kernel, bench.py --workload config3"},
+NCU_CAPTURE = {   # workload -> sieve launches per segment -> capture
+    "config2": {1: {"traffic": 290_849_280, "imad_pipe_busy": 0.782,
+                    "source": "ncu --set full capture of sieve_kernel, bench.py --segment 1e8"},
+                # the n-range in two launches: both launches of one 1e8-wide segment
+                # (29,672,960 and 73,291,520 B), averaged and scaled by 10; the first
+                # launch's 43 MB of residue state was still in L2 when it ended
+                2: {"traffic": 514_822_400, "imad_pipe_busy": 0.783,
+                    "source": "ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum of both sieve_kernel "
+                              "launches, bench.py --segment 1e8 --max-steps 50000"}},
+    "config3": {1: {"traffic": 18_765_568, "imad_pipe_busy": 0.836,
+                    "source": "ncu --set full capture of sieve_kernel, bench.py --workload config3"}},
 }
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 
@@ -120,7 +126,7 @@ def setup_products(fs, nmin: int, folded: bool = False):
     return plan, pow_d + 1 + 10 + 2 + 3
 
 
-def roofline(ctx, fs, wl, ncand, st, step_ms, clocks=None, seg=None):
+def roofline(ctx, fs, wl, ncand, st, step_ms, clocks=None, seg=None, segments=1):
     """Roofline of the fused sieve kernel.  The work is 64-bit modular
     multiplication: integer multiply-add, no memory traffic to speak of (the
     candidate list is read once).  The ceiling is the same arithmetic run
@@ -150,8 +156,13 @@ def roofline(ctx, fs, wl, ncand, st, step_ms, clocks=None, seg=None):
     lower_bound_s = ncand * (W / walk_ceil + plan_products / plan_ceil + mont_products / mm_ceil)
     achieved = pairs / sieve_s if sieve_s > 0 else 0.0
     peak = pairs / lower_bound_s if lower_bound_s > 0 else 0.0
-    cap = NCU_CAPTURE.get(wl, {})
-    alg_bytes = 8.0 * ncand / launches                  # the candidate list, read once
+    # launches per pass: 1 (setup, walk and check fused) or L > 1 when the n-range
+    # is split (the tuner's choice); each launch reads the candidate list, and
+    # between launches every candidate's residue and walked-n tag (12 bytes)
+    # are written and read back
+    per_pass = max(int(round(launches / max(segments, 1))), 1)
+    cap = NCU_CAPTURE.get(wl, {}).get(per_pass, {})
+    alg_bytes = (8.0 * per_pass + 24.0 * (per_pass - 1)) * ncand / launches
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -170,6 +181,7 @@ def roofline(ctx, fs, wl, ncand, st, step_ms, clocks=None, seg=None):
         "bound": "imad", "achieved": achieved / 1e9, "peak": peak / 1e9, "unit": "G pair-steps/s",
         "frac": achieved / peak if peak else None,
         "traffic": cap.get("traffic"), "algorithmic_bytes_per_launch": alg_bytes,
+        "launches_per_segment": per_pass,
         "kernel": "sieve_kernel (setup + walk + check fused)",
         "kernel_ms_per_launch": st["sieve_ms"] / launches,
         "share_of_step": st["sieve_ms"] / step_ms if step_ms else None,
@@ -400,6 +412,11 @@ def run_ours(args):
     # the launch shape: measured on a sample of this rank's share by the
     # library's tuner (fs_autotune) and applied to the context
     tune = ctx.autotune(lo, hi, nmin, nmax)
+    if args.max_steps is not None:
+        # a fixed n-range split (0: one launch per segment) over the tuned shape, for captures
+        t = dict(tune["tuning"], max_steps_per_launch=args.max_steps)
+        ctx.set_tuning(**t)
+        tune["tuning"] = t
     ctx.begin(pmin, pmax, nmin, nmax)
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
@@ -457,7 +474,7 @@ def run_ours(args):
     value = pairs / (ms * 1e-3)
 
     # roofline of the dominant kernel, from this rank's events
-    roof = roofline(ctx, fs, wl, my_pc, st, ms, clk.summary(), seg)
+    roof = roofline(ctx, fs, wl, my_pc, st, ms, clk.summary(), seg, segments=len(segs) * args.steps)
     # e2e through the public API with host buffers: every rank searches its
     # whole share with Context.sieve per step (plan upload, counters and hits
     # back, CPU verification), wall clock, max over ranks
@@ -582,7 +599,7 @@ def extra_config3(ctx, fs, torch, dev):
     ctx.set_timing(False)
     _, raw, pc, flags, rc = ctx.collect(1 << 20)
     want = fixture(wl)
-    roof = roofline(ctx, fs, wl, pc, st, ms, clk.summary(), seg)
+    roof = roofline(ctx, fs, wl, pc, st, ms, clk.summary(), seg, segments=len(segs))
     ctx.set_stream(None)
     t0 = time.perf_counter()
     r = ctx.sieve(segs[0][0], segs[0][1], nmin, nmax, threads=os.cpu_count() or 2)
@@ -766,6 +783,8 @@ def main():
     ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS) + ["config4", "config5"])
     ap.add_argument("--serve-seconds", type=float, default=180.0, help="config5: stop the replay after this long")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--max-steps", type=int, default=None,
+                    help="override the tuned n-steps per launch (0: the whole n-range in one launch)")
     ap.add_argument("--no-extra", action="store_true",
                     help="config2 at one GPU: skip the config1/config3/config4 sub-objects after the timed region")
     ap.add_argument("--segment", type=float, default=0,
