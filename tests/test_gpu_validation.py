@@ -86,3 +86,37 @@ def test_split_searches_pass_the_round_trip(ctx, orc, steps):
     finally:
         ctx.set_tuning()
     assert (r.primecount, r.raw_sum, r.checksum) == (want["primecount"], want["raw_sum"], want["checksum"])
+
+
+# one range per walk step (the regimes of tests/test_gpu_parity.py), each searched
+# with the n-range cut into short launches: every launch after the first starts
+# from stored residues and walked-n tags, and may take a different step as the
+# multipliers grow
+SPLIT_REGIMES = [
+    (10**15, 10**15 + 200_000, 100_000, 100_700),                  # half-offset 96-bit
+    (10**13, 10**13 + 30_000, 67_108_000, 67_109_700),             # half-offset 96-bit into lazy 96-bit at 2^26
+    ((1 << 63) + 1, (1 << 63) + 200_000, 5_000, 5_700),             # half-offset canonical 96-bit
+    ((1 << 63) + 1, (1 << 63) + 10_001, (1 << 26) - 300, (1 << 26) + 400),  # into canonical 96-bit at 2^26
+    ((1 << 64) - 200_000, (1 << 64) - 1, 1_000, 1_333),              # near 2^64
+    (10**12, 10**12 + 200_000, 100_000, 100_700),                  # float quotient
+    (10**12, 10**12 + 200_000, 441_000, 442_000),                  # float quotient into the lazy 64-bit step
+    ((1 << 34) + 1, (1 << 34) + 200_001, 20_000, 20_900),          # shifted-window 64-bit
+    ((1 << 31) - 100_000, (1 << 31) + 100_000, 2000, 2900),         # 32-bit / shifted-window boundary
+    (10**9, 10**9 + 20_000, 67_108_000, 67_109_000),               # 32-bit step into the generic walk
+    ((1 << 33) - 100_000, (1 << 33) + 100_000, 2000, 2900),         # generic / lazy boundary
+    (1_000_000, 1_100_000, 1000, 3000),                            # small p, many hits
+]
+
+
+@pytest.mark.parametrize("lo,hi,nmin,nmax", SPLIT_REGIMES)
+@pytest.mark.parametrize("steps", [97, 1000])
+def test_split_walks_in_every_regime_equal_the_oracle(ctx, orc, lo, hi, nmin, nmax, steps):
+    want = orc.run(lo, hi, nmin, nmax)
+    assert want["status"] == 0
+    ctx.set_tuning(max_steps_per_launch=steps)
+    try:
+        r = ctx.sieve(lo, hi, nmin, nmax)
+    finally:
+        ctx.set_tuning()
+    assert (r.primecount, r.raw_sum, r.checksum, r.factorcount) == \
+        (want["primecount"], want["raw_sum"], want["checksum"], want["factorcount"])
