@@ -410,8 +410,11 @@ def run_ours(args):
             ctx.segment(s_lo, s_hi)
 
     # the launch shape: measured on a sample of this rank's share by the
-    # library's tuner (fs_autotune) and applied to the context
-    tune = ctx.autotune(lo, hi, nmin, nmax)
+    # library's tuner (fs_autotune) and applied to the context, tuned for the
+    # work of a run of at least 20 passes over the share (its samples take
+    # about a tenth of that; the tuning is outside the timed region)
+    passes = max(args.warmup + args.steps, 20)
+    tune = ctx.autotune(lo, min(lo + (hi - lo) * passes, (1 << 64) - 1), nmin, nmax)
     if args.max_steps is not None:
         # a fixed n-range split (0: one launch per segment) over the tuned shape, for captures
         t = dict(tune["tuning"], max_steps_per_launch=args.max_steps)
@@ -576,7 +579,9 @@ def extra_config3(ctx, fs, torch, dev):
     stream = torch.cuda.Stream(device=dev)
     ctx.set_stream(stream.cuda_stream)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    tune = ctx.autotune(pmin, pmax, nmin, nmax)
+    # tuned as for a 20-pass run of this workload (the two passes below alone
+    # are too short for the tuner to spend its samples on)
+    tune = ctx.autotune(pmin, pmin + (pmax - pmin) * 20, nmin, nmax)
     ctx.begin(pmin, pmax, nmin, nmax)
     with torch.cuda.stream(stream):
         for s_lo, s_hi in segs:

@@ -221,16 +221,18 @@ extern "C" int fs_autotune(fs_ctx* c, uint64_t pmin, uint64_t pmax, uint32_t nmi
     }
     // the sample: the range's first p-values, at least about 2e11 units of
     // work (a tenth of a second on a GB300) and three passes of the largest
-    // grid tried (so the last partial pass does not decide), at most a
-    // quarter of the whole run
+    // grid tried (so the last partial pass does not decide); the ten or so
+    // samples together stay near a tenth of the whole run, and a run too
+    // short for that keeps the defaults
     const uint32_t W = nmax - nmin;
     const double words = (double)fs::build_plan(nmin, 1).words.size();
     const double per_cand = (double)W + 2.7 * words + 64.0;   // walk steps + setup, in walk-step units
     const double pass = (double)c->sm_count * c->sieve_occ[5] * 4 * 256 * 4;
-    const double sample_cands = std::min(std::max(2e11 / per_cand, 3 * pass), est_cands(pmin, pmax) / 4);
+    const double want = std::max(2e11 / per_cand, 3 * pass);
+    const double sample_cands = want <= est_cands(pmin, pmax) / 100 ? want : 0.0;
     const uint32_t batch_tile = c->tuning.batch_tile_candidates;
     if (sample_cands < 20000) {
-        // too small a run to time: the defaults
+        // too short a run to time: the defaults
         fs_tuning t{};
         t.batch_tile_candidates = batch_tile;
         if ((rc = fs_set_tuning(c, &t))) return rc;

@@ -165,7 +165,9 @@ int fs_batch_release(fs_ctx *ctx);
  * 5), blocks per SM (1x, 2x, 4x the resident ones), threads per block (256 or
  * 128), n-steps per launch (all, or halves) -- applies the fastest to the
  * context and sizes a segment to about target_ms (<= 0: 1000) of kernel time
- * at the measured rate.  The choice is cached in the text file cache_path
+ * at the measured rate.  The samples together take about a tenth of the
+ * run's work; a run too short for that keeps the default shape (nothing is
+ * timed, shapes_tried = 0).  The choice is cached in the text file cache_path
  * (NULL: no cache) under the GPU name, SM count and the workload's bucket
  * (log2 of the n-width, of p and of nmin); a cached choice is applied without
  * timing.  Runs its own sample searches on the context: call it before

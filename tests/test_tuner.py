@@ -1,36 +1,51 @@
 """The native tuner (fs_autotune, fs_autotune_batch): it times launch shapes
 on a sample, applies the fastest, caches the choice per GPU and workload
 bucket, and never changes results."""
+import os
+
 import pytest
 
 from factsieve_gb300 import tuner
 
 pytestmark = pytest.mark.gpu
 
-SEARCH = (10**12, 10**12 + 30_000_000, 100_000, 101_000)
+# a run long enough to tune (its samples take about a tenth of it)
+LONG = (10**12, 10**12 + 3 * 10**10, 100_000, 200_000)
+CHECK = (10**12, 10**12 + 3_000_000, 100_000, 200_000)
 
 
 def test_tuned_search_gives_identical_results_and_is_cached(ctx, tmp_path):
     cache = str(tmp_path / "tuning.txt")
-    base = ctx.sieve(*SEARCH)
-    best = tuner.autotune(ctx, *SEARCH, target_ms=500, cache_path=cache)
+    base = ctx.sieve(*CHECK)
+    best = tuner.autotune(ctx, *LONG, target_ms=500, cache_path=cache)
     try:
         assert best["shapes_tried"] >= 6 and best["rate"] > 0 and not best["from_cache"]
         t = best["tuning"]
         assert t["sieve_variant"] in (3, 5) and t["sieve_block_threads"] in (128, 256)
         assert ctx.tuning()["sieve_variant"] == t["sieve_variant"]        # applied to the context
         assert 1e5 <= best["seg_width"] <= 4_294_900_000
-        assert best["steps_per_launch"] in (1000, 500)
-        tuned = ctx.sieve(*SEARCH, seg_width=best["seg_width"])
+        assert best["steps_per_launch"] in (100_000, 50_000)
+        tuned = ctx.sieve(*CHECK, seg_width=best["seg_width"])
         assert (tuned.raw_sum, tuned.primecount, tuned.checksum) == (base.raw_sum, base.primecount, base.checksum)
         # the same bucket again: read from the cache, nothing timed
-        again = tuner.autotune(ctx, 10**12 + 7, 10**12 + 20_000_000, 100_003, 101_003, cache_path=cache)
+        again = tuner.autotune(ctx, 10**12 + 7, 10**12 + 4 * 10**10, 100_003, 200_003, cache_path=cache)
         assert again["from_cache"] == 1 and again["shapes_tried"] == 0
         assert again["tuning"] == best["tuning"]
         lines = open(cache).read().splitlines()
         assert len(lines) == 1 and lines[0].startswith("search|")
     finally:
         ctx.set_tuning()
+
+
+def test_a_short_run_keeps_the_defaults(ctx, tmp_path):
+    """A search whose samples would be more than about a tenth of it is not
+    timed: the default shape, a segment width from the planning rate."""
+    cache = str(tmp_path / "tuning.txt")
+    r = tuner.autotune(ctx, 10**12, 10**12 + 30_000_000, 100_000, 101_000, cache_path=cache)
+    assert (r["shapes_tried"], r["rate"], r["from_cache"]) == (0, 0.0, 0)
+    assert r["tuning"]["sieve_variant"] == 5 and r["tuning"]["max_steps_per_launch"] == 0
+    assert 1e5 <= r["seg_width"] <= 30_000_000
+    assert not os.path.exists(cache)                                 # nothing measured, nothing cached
 
 
 @pytest.mark.parametrize("shape", [
