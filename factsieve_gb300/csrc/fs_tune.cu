@@ -332,7 +332,10 @@ extern "C" int fs_autotune_batch(fs_ctx* c, const fs_job* jobs, uint32_t njobs, 
     // the mix with every p-range narrowed scale_down times: the same n-ranges
     // and setup plans, fewer candidates per job
     std::vector<fs_job> sample(jobs, jobs + njobs);
-    for (auto& j : sample) j.pmax = j.pmin + std::max<uint64_t>((j.pmax - j.pmin) / scale_down, 10000);
+    for (auto& j : sample) {
+        const uint64_t w = std::max<uint64_t>((j.pmax - j.pmin) / scale_down, 10000);
+        j.pmax = j.pmin + w < j.pmin ? ~0ull : j.pmin + w;   // no wrap past 2^64
+    }
     const SavedStats saved = save_stats(c);
     uint32_t best_tile = fs::kTileCandidates;
     double best_ms = -1;
