@@ -101,6 +101,9 @@ def reference_setup_products(nmin: int) -> int:
 # Ceiling microkernels (fs_bench_int_pipe kinds) of each residue step.
 STEP_CEILING_KIND = {6: (11, "32-bit half-offset step"), 7: (12, "shifted-window half-offset 64-bit step"),
                      9: (14, "half-offset 64-bit step, quotient on the FP32 pipe"),
+                     10: (16, "half-offset 64-bit step, FP32 quotient over a k_max-sized window, s >= 32"),
+                     11: (17, "half-offset 64-bit step, FP32 quotient over a k_max-sized window, s <= 32"),
+                     12: (18, "half-offset 96-bit step, FP32 quotient over a k_max-sized window"),
                      4: (5, "half-offset lazy 64-bit step"),
                      5: (10, "half-offset lazy 96-bit step"), 8: (13, "half-offset canonical 96-bit step"),
                      1: (6, "lazy 64-bit step"),

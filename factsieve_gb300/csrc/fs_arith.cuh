@@ -665,6 +665,158 @@ __device__ __forceinline__ u32 halff_walk8x2(u32& al, u32& ah, u32& bl, u32& bh,
     return flag;
 }
 
+// ------- iterate: half-offset steps, float quotient with a k_max-aware window --
+//
+// The float quotient of halff_walk8x2 with the window chosen from the
+// multipliers as well: for each candidate, T = ceil(23 p k_max / 16) bounds
+// t = r k while r < (23/16) p, s = bitlen(T) - 24 keeps z = floor(t / 2^s)
+// below 2^24, and g = m 2^(s-e) (m = floor(2^e / p), e = bitlen(p) + 23)
+// turns z into the estimate q = floor(z g) with one round-down FMA on the
+// subnormal grid (an integer below 2^24 read as a float is z 2^-149: exponent
+// field 0 or 1, both with spacing 2^-149).  Then q <= t/p and t/p - q <
+// 1 + 2^s/p + (t/p) 2^-23 < 1 + (46/16) k_max 2^-23, so for 46 k_max < 7 2^23
+// the residue stays below (23/16) p < x + p from a canonical start, and the
+// hit test is the half-offset one, r in {x, x + 1}.  Three forms:
+//   HG    t < 2^64, s >= 32: z = (t's high word) >> (s - 32) (the
+//         halff_walk8x2 block with this window);
+//   HGL   t < 2^64, s <= 32: z = the funnel shift of t's two words by s;
+//   HG96  p < 2^63, t up to 96 bits, s >= 32: z = the funnel shift of t's
+//         upper two words by s - 32, r' = t + q (2^64 - p) modulo 2^64.
+// The host picks one for a whole launch (walk_for_range) when every
+// candidate's s falls on its side of 32.
+constexpr u32 kHalfGMaxK = 1276526;   // 46 k_max < 7 2^23 with a margin for the rounding of T
+
+__device__ __forceinline__ int halfg_window(u64 p, u32 kmax) {
+    const unsigned __int128 T = ((unsigned __int128)23 * p * kmax + 15) / 16;
+    const u64 th = (u64)(T >> 64), tl = (u64)T;
+    return (th ? 128 - __clzll(th) : 64 - __clzll(tl)) - 24;
+}
+
+// form: 0 HG (sh = s - 32), 1 HGL (sh = s), 2 HG96 (sh = s - 32)
+__device__ __forceinline__ HalfF make_halfg(const Prime& c, u32 kmax, int form) {
+    HalfF H;
+    H.p = c.p;
+    H.x = (c.p - 1) >> 1;
+    const u64 np = 0ull - c.p;
+    H.np0 = (u32)np;
+    H.np1 = (u32)(np >> 32);
+    const int bl = bitlen64(c.p), e = bl + 23, s = halfg_window(c.p, kmax);
+    const u32 m = e <= 64 ? (u32)(((~0ull) / c.p) >> (64 - e)) : recip_pow2(c.p, e);
+    H.g = __uint_as_float(((u32)(s - e + 149) << 23) + m);
+    H.sh = (u32)(form == 1 ? s : s - 32);
+    H.x0 = (u32)H.x;
+    H.x1 = (u32)(H.x + 1);
+    return H;
+}
+
+// floor(z g) for a window z < 2^24.
+__device__ __forceinline__ u32 halfg_quot(u32 z, const HalfF& H) {
+    u32 q;
+    asm("{\n\t"
+        ".reg .f32 f;\n\t"
+        "mov.b32 f, %1;\n\t"
+        "fma.rm.f32 f, f, %2, 0f00000000;\n\t"
+        "mov.b32 %0, f;\n\t"
+        "}"
+        : "=r"(q)
+        : "r"(z), "f"(H.g));
+    return q;
+}
+
+__device__ __forceinline__ u64 halfgl_step(u64 r, u32 k, const HalfF& H) {
+    const u64 t = r * (u64)k;
+    const u32 q = halfg_quot((u32)(t >> H.sh), H);
+    return t + (u64)q * (((u64)H.np1 << 32) | H.np0);
+}
+
+__device__ __forceinline__ u64 halfg96_step(u64 r, u32 k, const HalfF& H) {
+    const unsigned __int128 t = (unsigned __int128)r * k;
+    const u32 q = halfg_quot((u32)(t >> (H.sh + 32)), H);
+    return (u64)t + (u64)q * (((u64)H.np1 << 32) | H.np0);
+}
+
+#define FS_HGL_MUL(RL, RH, NP0, NP1, G, SH, T, TL, TH, Z, Q, F)      \
+    "mul.wide.u32 " T ", " RL ", kk;\n\t"                          \
+    "mov.b64 {" TL ", " TH "}, " T ";\n\t"                         \
+    "mad.lo.u32 " TH ", " RH ", kk, " TH ";\n\t"                   \
+    "shf.r.clamp.b32 " Z ", " TL ", " TH ", " SH ";\n\t"           \
+    "mov.b32 " F ", " Z ";\n\t"                                    \
+    "fma.rm.f32 " F ", " F ", " G ", 0f00000000;\n\t"              \
+    "mov.b32 " Q ", " F ";\n\t"                                    \
+    "mad.lo.cc.u32 " RL ", " Q ", " NP0 ", " TL ";\n\t"            \
+    "madc.hi.u32 " TH ", " Q ", " NP0 ", " TH ";\n\t"              \
+    "mad.lo.u32 " RH ", " Q ", " NP1 ", " TH ";\n\t"
+#define FS_HGL_STEP2(J)                                                                  \
+    "add.u32 kk, %5, " #J ";\n\t"                                                        \
+    FS_HF_TEST("%0", "%10", "%11")                                                       \
+    FS_HF_TEST("%2", "%16", "%17")                                                       \
+    FS_HGL_MUL("%0", "%1", "%6", "%7", "%8", "%9", "TA", "aL", "aH", "az", "aq", "fa")   \
+    FS_HGL_MUL("%2", "%3", "%12", "%13", "%14", "%15", "TB", "bL", "bH", "bz", "bq", "fb")
+
+// Eight HGL steps on two residues; the flag as lazy_walk8x2's.
+__device__ __forceinline__ u32 halfgl_walk8x2(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const HalfF& A,
+                                              const HalfF& B) {
+    u32 flag;
+    asm("{\n\t"
+        ".reg .u32 kk, aL, aH, az, aq, bL, bH, bz, bq;\n\t"
+        ".reg .f32 fa, fb;\n\t"
+        ".reg .u64 TA, TB;\n\t"
+        ".reg .pred P;\n\t"
+        "setp.ne.u32 P, %5, %5;\n\t"
+        FS_HGL_STEP2(0) FS_HGL_STEP2(1) FS_HGL_STEP2(2) FS_HGL_STEP2(3)
+        FS_HGL_STEP2(4) FS_HGL_STEP2(5) FS_HGL_STEP2(6) FS_HGL_STEP2(7)
+        "selp.u32 %4, 1, 0, P;\n\t"
+        "}"
+        : "+r"(al), "+r"(ah), "+r"(bl), "+r"(bh), "=r"(flag)
+        : "r"(k1), "r"(A.np0), "r"(A.np1), "f"(A.g), "r"(A.sh), "r"(A.x0), "r"(A.x1),
+          "r"(B.np0), "r"(B.np1), "f"(B.g), "r"(B.sh), "r"(B.x0), "r"(B.x1));
+    return flag;
+}
+
+// The 96-bit multiply of half96_walk8x2 (mad.wide with 64-bit addends) with
+// the float quotient.
+#define FS_HG96_MUL(RL, RH, NP0, NP1, G, SH, T, U, R, CC, T0, C, T1, T2, Z, Q, F)  \
+    "mul.wide.u32 " T ", " RL ", kk;\n\t"                                        \
+    "mov.b64 {" T0 ", " C "}, " T ";\n\t"                                        \
+    "mov.b64 " CC ", {" C ", zr};\n\t"                                           \
+    "mad.wide.u32 " U ", " RH ", kk, " CC ";\n\t"                                \
+    "mov.b64 {" T1 ", " T2 "}, " U ";\n\t"                                       \
+    "shf.r.clamp.b32 " Z ", " T1 ", " T2 ", " SH ";\n\t"                         \
+    "mov.b32 " F ", " Z ";\n\t"                                                  \
+    "fma.rm.f32 " F ", " F ", " G ", 0f00000000;\n\t"                            \
+    "mov.b32 " Q ", " F ";\n\t"                                                  \
+    "mov.b64 " T ", {" T0 ", " T1 "};\n\t"                                       \
+    "mad.wide.u32 " R ", " Q ", " NP0 ", " T ";\n\t"                             \
+    "mov.b64 {" RL ", " RH "}, " R ";\n\t"                                       \
+    "mad.lo.u32 " RH ", " Q ", " NP1 ", " RH ";\n\t"
+#define FS_HG96_STEP2(J)                                                                       \
+    "add.u32 kk, %5, " #J ";\n\t"                                                              \
+    FS_HF_TEST("%0", "%10", "%11")                                                             \
+    FS_HF_TEST("%2", "%16", "%17")                                                             \
+    FS_HG96_MUL("%0", "%1", "%6", "%7", "%8", "%9", "TA", "UA", "RA", "CA", "a0", "ac", "a1", "a2", "az", "aq", "fa") \
+    FS_HG96_MUL("%2", "%3", "%12", "%13", "%14", "%15", "TB", "UB", "RB", "CB", "b0", "bc", "b1", "b2", "bz", "bq", "fb")
+
+// Eight HG96 steps on two residues; the flag as lazy_walk8x2's.
+__device__ __forceinline__ u32 halfg96_walk8x2(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const HalfF& A,
+                                               const HalfF& B) {
+    u32 flag;
+    asm("{\n\t"
+        ".reg .u32 kk, zr, a0, ac, a1, a2, az, aq, b0, bc, b1, b2, bz, bq;\n\t"
+        ".reg .f32 fa, fb;\n\t"
+        ".reg .u64 TA, UA, RA, CA, TB, UB, RB, CB;\n\t"
+        ".reg .pred P;\n\t"
+        "mov.u32 zr, 0;\n\t"
+        "setp.ne.u32 P, %5, %5;\n\t"
+        FS_HG96_STEP2(0) FS_HG96_STEP2(1) FS_HG96_STEP2(2) FS_HG96_STEP2(3)
+        FS_HG96_STEP2(4) FS_HG96_STEP2(5) FS_HG96_STEP2(6) FS_HG96_STEP2(7)
+        "selp.u32 %4, 1, 0, P;\n\t"
+        "}"
+        : "+r"(al), "+r"(ah), "+r"(bl), "+r"(bh), "=r"(flag)
+        : "r"(k1), "r"(A.np0), "r"(A.np1), "f"(A.g), "r"(A.sh), "r"(A.x0), "r"(A.x1),
+          "r"(B.np0), "r"(B.np1), "f"(B.g), "r"(B.sh), "r"(B.x0), "r"(B.x1));
+    return flag;
+}
+
 // ------------------------- iterate: lazy 96-bit steps, half-offset form --
 //
 // The half-offset form for the lazy 96-bit step.  With the window z = t >> s
@@ -842,7 +994,9 @@ __device__ __forceinline__ Half96 make_halfmid(const Prime& c, u32 kmax) {
     const int s0 = bitlen64(c.p) + bitlen32(kmax) - 29;
     const int s = s0 > 0 ? s0 : 0;
     H.sh = (u32)s;
-    H.M = (u32)((1ull << (32 + s)) / c.p);
+    // s reaches 32 (p >= 2^35 with k_max >= 2^24), where 1 << (32 + s) would
+    // overflow: floor((2^(32+s) - 1) / p) is the same quotient for odd p > 1
+    H.M = (u32)((~0ull >> (32 - s)) / c.p);
     H.x0 = (u32)H.x;
     H.x1 = (u32)(H.x + 1);
     return H;

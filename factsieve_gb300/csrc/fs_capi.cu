@@ -778,7 +778,9 @@ int fs_walk_step(uint64_t plo, uint64_t phi, uint32_t kmax) { return fs::walk_fo
 int fs_setup_form(uint64_t plo, uint64_t phi) { return fs::pm_setup_for_range(plo, phi); }
 
 int fs_bench_int_pipe(fs_ctx* c, uint32_t kind, uint32_t iters, double* ops_per_sec, double* ms) {
-    if (!c || kind > 15 || iters == 0 || iters > (1u << 24)) return FS_E_ARG;
+    if (!c || kind > 18 || iters == 0 || iters > (1u << 24)) return FS_E_ARG;
+    // kinds 16-18 walk multipliers up to 100001 + 8 iters, within their k_max bound
+    if (kind >= 16 && 100001u + 8u * iters > 1276526u) return FS_E_ARG;
     int rc = bind(c);
     if (rc) return rc;
     const int grid = c->sm_count * 8;   // 8 x 256 threads = 2048 per SM

@@ -252,7 +252,10 @@ __global__ void __launch_bounds__(256) imad_bench_kernel(u32 iters, u32 kind, u3
 //   kind 13 half-offset canonical 96-bit steps (canon96h_walk8x2), 4 chains
 //   kind 14 half-offset 64-bit steps, quotient on the FP32 pipe (halff_walk8x2), 4 chains
 //   kind 15 folding products modulo p = 2^63 + d (pm_mul), 8 chains
-constexpr u32 kCeilUnits[16] = {0, 0, 0, 0, 8, 32, 32, 32, 32, 4, 32, 32, 32, 32, 32, 8};
+//   kind 16 float-quotient steps, k_max-aware window, s >= 32 (HG: halff_walk8x2), 4 chains
+//   kind 17 the same with s <= 32 (HGL: halfgl_walk8x2), 4 chains
+//   kind 18 the same with a 96-bit t (HG96: halfg96_walk8x2), 4 chains
+constexpr u32 kCeilUnits[19] = {0, 0, 0, 0, 8, 32, 32, 32, 32, 4, 32, 32, 32, 32, 32, 8, 32, 32, 32};
 
 template <u32 kind>
 __global__ void __launch_bounds__(256) ceiling_kernel(u32 iters, u32 seed, u32* sink) {
@@ -262,6 +265,9 @@ __global__ void __launch_bounds__(256) ceiling_kernel(u32 iters, u32 seed, u32* 
     switch (kind) {
         case 5: base = 1000000000000ull; break;           // 2^36 <= p, p kmax <= 2^62
         case 14: base = 1000000000000ull; break;          // 2^38 <= p, 19 p kmax < 2^(bitlen(p) + 23)
+        case 16: base = 1000000000000ull; break;          // window shift s >= 32, t < 2^64
+        case 17: base = (1ull << 34) + 1; break;          // window shift s <= 32
+        case 18: base = 1000000000000000ull; break;       // t beyond 2^64, p < 2^63
         case 6: base = (1ull << 34) + 1; break;           // 2^33 < p < 2^36
         case 7: base = 1000000000000000ull; break;        // p kmax > 2^62, p < 2^63
         case 10: base = 1000000000000000ull; break;       // p kmax > 2^60, p < 2^63
@@ -340,6 +346,23 @@ __global__ void __launch_bounds__(256) ceiling_kernel(u32 iters, u32 seed, u32* 
             for (u32 it = 0; it < iters; ++it) {
                 acc += halff_walk8x2(l[0], hh[0], l[1], hh[1], k0 + 8 * it, A, B);
                 acc += halff_walk8x2(l[2], hh[2], l[3], hh[3], k0 + 8 * it, C, D);
+            }
+        } else if constexpr (kind == 16 || kind == 17 || kind == 18) {
+            const u32 kmax = k0 + 8 * iters;
+            const int form = kind == 16 ? 0 : (kind == 17 ? 1 : 2);
+            const HalfF A = make_halfg(c[0], kmax, form), B = make_halfg(c[1], kmax, form);
+            const HalfF C = make_halfg(c[2], kmax, form), D = make_halfg(c[3], kmax, form);
+            for (u32 it = 0; it < iters; ++it) {
+                if constexpr (kind == 16) {
+                    acc += halff_walk8x2(l[0], hh[0], l[1], hh[1], k0 + 8 * it, A, B);
+                    acc += halff_walk8x2(l[2], hh[2], l[3], hh[3], k0 + 8 * it, C, D);
+                } else if constexpr (kind == 17) {
+                    acc += halfgl_walk8x2(l[0], hh[0], l[1], hh[1], k0 + 8 * it, A, B);
+                    acc += halfgl_walk8x2(l[2], hh[2], l[3], hh[3], k0 + 8 * it, C, D);
+                } else {
+                    acc += halfg96_walk8x2(l[0], hh[0], l[1], hh[1], k0 + 8 * it, A, B);
+                    acc += halfg96_walk8x2(l[2], hh[2], l[3], hh[3], k0 + 8 * it, C, D);
+                }
             }
         } else if constexpr (kind == 6) {
             const Lazy64 A = make_lazy(c[0]), B = make_lazy(c[1]), C = make_lazy(c[2]), D = make_lazy(c[3]);
@@ -436,12 +459,22 @@ cudaError_t launch_imad_bench(u32 iters, u32 kind, u32 seed, u32* sink, int grid
         case 13: ceiling_kernel<13><<<grid, 256, 0, s>>>(iters, seed, sink); break;
         case 14: ceiling_kernel<14><<<grid, 256, 0, s>>>(iters, seed, sink); break;
         case 15: ceiling_kernel<15><<<grid, 256, 0, s>>>(iters, seed, sink); break;
+        case 16: ceiling_kernel<16><<<grid, 256, 0, s>>>(iters, seed, sink); break;
+        case 17: ceiling_kernel<17><<<grid, 256, 0, s>>>(iters, seed, sink); break;
+        case 18: ceiling_kernel<18><<<grid, 256, 0, s>>>(iters, seed, sink); break;
         default: imad_bench_kernel<<<grid, 256, 0, s>>>(iters, kind, seed, sink); break;
     }
     return cudaGetLastError();
 }
 
-double bench_units_per_thread_iter(u32 kind) { return kind < 4 ? 8.0 : (kind < 16 ? kCeilUnits[kind] : 0.0); }
+double bench_units_per_thread_iter(u32 kind) { return kind < 4 ? 8.0 : (kind < 19 ? kCeilUnits[kind] : 0.0); }
+
+// bitlen(ceil(23 p kmax / 16)) - 24: the window shift of make_halfg.
+static int halfg_window_host(uint64_t p, uint32_t kmax) {
+    const unsigned __int128 T = ((unsigned __int128)23 * p * kmax + 15) / 16;
+    const uint64_t th = (uint64_t)(T >> 64), tl = (uint64_t)T;
+    return (th ? 128 - __builtin_clzll(th) : 64 - __builtin_clzll(tl)) - 24;
+}
 
 int walk_for_range(uint64_t plo, uint64_t phi, uint32_t kmax) {
     if (phi <= plo || kmax == 0) return WALK_ANY;
@@ -449,8 +482,6 @@ int walk_for_range(uint64_t plo, uint64_t phi, uint32_t kmax) {
     const int kb = 32 - __builtin_clz(kmax);
     // the 32-bit half-offset step needs 2 < p < 2^31 and kmax < 2^26 (half32_ok)
     if (plo > 2 && pmax < (1ull << 31) && kb <= 26) return WALK_H32;
-    // the shifted-window half-offset step needs 2^31 <= p < 2^36 and kmax < 2^25 (halfmid_ok)
-    if (plo >= (1ull << 31) && pmax < (1ull << 36) && kb <= 25) return WALK_HM;
     // the float-quotient half-offset step needs p >= 2^38, p kmax <= 2^62,
     // 19 kmax <= 2^23 and 19 pmax kmax < 2^(bitlen(plo) + 23) (the bounds
     // of halff_walk8x2 with s taken from a thread's least candidate; launch-
@@ -458,6 +489,21 @@ int walk_for_range(uint64_t plo, uint64_t phi, uint32_t kmax) {
     if (plo >= (1ull << 38) && pmax <= ((1ull << 62) / kmax) && 19ull * kmax <= (1ull << 23) &&
         (unsigned __int128)19 * pmax * kmax < ((unsigned __int128)1 << ((64 - __builtin_clzll(plo)) + 23)))
         return WALK_HF;
+    // the float-quotient steps with a k_max-aware window (make_halfg) need
+    // p >= 2^31 and 46 kmax < 7 2^23, and every candidate's window shift
+    // s = bitlen(ceil(23 p kmax / 16)) - 24 on one side of 32: s <= 32 with
+    // t < 2^64 (HGL), s >= 32 with t < 2^64 (HG), s in [32, 64) with p < 2^63
+    // (HG96, t up to 96 bits)
+    if (plo >= (1ull << 31) && kmax <= kHalfGMaxK) {
+        const int slo = halfg_window_host(plo, kmax), shi = halfg_window_host(pmax, kmax);
+        const bool t64 = ((unsigned __int128)23 * pmax * kmax + 15) / 16 < ((unsigned __int128)1 << 64);
+        if (t64 && shi <= 32) return WALK_HGL;
+        if (t64 && slo >= 32) return WALK_HG;
+        if (slo >= 32 && shi < 64 && (pmax >> 63) == 0) return WALK_HG96;
+    }
+    // the shifted-window half-offset step needs 2^31 <= p < 2^36 and kmax < 2^25 (halfmid_ok);
+    // HGL runs the same range 14 % faster and is taken first where it holds
+    if (plo >= (1ull << 31) && pmax < (1ull << 36) && kb <= 25) return WALK_HM;
     // the half-offset lazy step needs p >= 2^36 and p kmax <= 2^62 (half_ok)
     if (plo >= (1ull << 36) && pmax <= ((1ull << 62) / kmax)) return WALK_H64;
     // the lazy 64-bit step needs p > 2^33 and p kmax <= 2^62 (lazy_ok)

@@ -23,6 +23,9 @@ cudaError_t launch_sieve_pair(const SieveArgs& a, int setup, bool final_chunk, i
     if (threads != kSieveThreads && threads != kSieveThreads / 2) return cudaErrorInvalidValue;
     switch (walk) {
         case WALK_HF: launch_sieve_w<3, WALK_HF>(a, setup, final_chunk, grid, s, threads); break;
+        case WALK_HG: launch_sieve_w<3, WALK_HG>(a, setup, final_chunk, grid, s, threads); break;
+        case WALK_HGL: launch_sieve_w<3, WALK_HGL>(a, setup, final_chunk, grid, s, threads); break;
+        case WALK_HG96: launch_sieve_w<3, WALK_HG96>(a, setup, final_chunk, grid, s, threads); break;
         case WALK_H64: launch_sieve_w<3, WALK_H64>(a, setup, final_chunk, grid, s, threads); break;
         case WALK_H96: launch_sieve_w<3, WALK_H96>(a, setup, final_chunk, grid, s, threads); break;
         case WALK_H32: launch_sieve_w<3, WALK_H32>(a, setup, final_chunk, grid, s, threads); break;

@@ -30,6 +30,9 @@ cudaError_t launch_sieve_quad(const SieveArgs& a, int setup, bool final_chunk, i
     if (threads != kSieveThreads && threads != kSieveThreads / 2) return cudaErrorInvalidValue;
     switch (walk) {
         case WALK_HF: launch_sieve_w<2, WALK_HF, 4>(a, setup, final_chunk, grid, s, threads); break;
+        case WALK_HG: launch_sieve_w<2, WALK_HG, 4>(a, setup, final_chunk, grid, s, threads); break;
+        case WALK_HGL: launch_sieve_w<2, WALK_HGL, 4>(a, setup, final_chunk, grid, s, threads); break;
+        case WALK_HG96: launch_sieve_w<2, WALK_HG96, 4>(a, setup, final_chunk, grid, s, threads); break;
         case WALK_H64: launch_sieve_w<2, WALK_H64, 4>(a, setup, final_chunk, grid, s, threads); break;
         case WALK_H96: launch_sieve_w<2, WALK_H96, 4>(a, setup, final_chunk, grid, s, threads); break;
         case WALK_H32: launch_sieve_w<2, WALK_H32, 4>(a, setup, final_chunk, grid, s, threads); break;

@@ -298,6 +298,50 @@ struct RegHF {
     }
     static __device__ __forceinline__ int hit(u64 c, const K& X) { return c == X.x ? -1 : (c == X.x + 1 ? 1 : 0); }
 };
+// The float quotient with the window chosen from k_max (make_halfg): HG on
+// the halff_walk8x2 block, HGL and HG96 on their own blocks.
+struct RegHG {
+    using K = HalfF;
+    static __device__ __forceinline__ K make(const Prime& c, u32 kmax, u64) { return make_halfg(c, kmax, 0); }
+    static __device__ __forceinline__ u32 block(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const K& A, const K& B) {
+        return halff_walk8x2(al, ah, bl, bh, k1, A, B);
+    }
+    static __device__ __forceinline__ u64 step(u64 r, u32 k, const K& X) { return halff_step(r, k, X); }
+    static __device__ __forceinline__ u64 canon(u64 r, const K& X) { return halff_canon(r, X); }
+    static __device__ __forceinline__ u64 enter(u64 r, const Prime& c, const K& X) { return half_enter(r, c, X.x); }
+    static __device__ __forceinline__ u64 leave(u64 r, const Prime& c, const K& X) {
+        return half_leave(halff_canon(r, X), c);
+    }
+    static __device__ __forceinline__ int hit(u64 c, const K& X) { return c == X.x ? -1 : (c == X.x + 1 ? 1 : 0); }
+};
+struct RegHGL {
+    using K = HalfF;
+    static __device__ __forceinline__ K make(const Prime& c, u32 kmax, u64) { return make_halfg(c, kmax, 1); }
+    static __device__ __forceinline__ u32 block(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const K& A, const K& B) {
+        return halfgl_walk8x2(al, ah, bl, bh, k1, A, B);
+    }
+    static __device__ __forceinline__ u64 step(u64 r, u32 k, const K& X) { return halfgl_step(r, k, X); }
+    static __device__ __forceinline__ u64 canon(u64 r, const K& X) { return halff_canon(r, X); }
+    static __device__ __forceinline__ u64 enter(u64 r, const Prime& c, const K& X) { return half_enter(r, c, X.x); }
+    static __device__ __forceinline__ u64 leave(u64 r, const Prime& c, const K& X) {
+        return half_leave(halff_canon(r, X), c);
+    }
+    static __device__ __forceinline__ int hit(u64 c, const K& X) { return c == X.x ? -1 : (c == X.x + 1 ? 1 : 0); }
+};
+struct RegHG96 {
+    using K = HalfF;
+    static __device__ __forceinline__ K make(const Prime& c, u32 kmax, u64) { return make_halfg(c, kmax, 2); }
+    static __device__ __forceinline__ u32 block(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const K& A, const K& B) {
+        return halfg96_walk8x2(al, ah, bl, bh, k1, A, B);
+    }
+    static __device__ __forceinline__ u64 step(u64 r, u32 k, const K& X) { return halfg96_step(r, k, X); }
+    static __device__ __forceinline__ u64 canon(u64 r, const K& X) { return halff_canon(r, X); }
+    static __device__ __forceinline__ u64 enter(u64 r, const Prime& c, const K& X) { return half_enter(r, c, X.x); }
+    static __device__ __forceinline__ u64 leave(u64 r, const Prime& c, const K& X) {
+        return half_leave(halff_canon(r, X), c);
+    }
+    static __device__ __forceinline__ int hit(u64 c, const K& X) { return c == X.x ? -1 : (c == X.x + 1 ? 1 : 0); }
+};
 struct RegH32 {
     using K = Half32;
     static __device__ __forceinline__ K make(const Prime& c, u32 kmax, u64) { return make_half32(c, kmax); }
@@ -495,6 +539,9 @@ __device__ __forceinline__ void walk_pair_as(u64& ra, u64& rb, const Prime& a, c
                                              u32 nstart, u32 nend, const WalkOut& o) {
     if (nstart >= nend) return;
     if (WALK == WALK_HF) walk_reg_pair<RegHF>(ra, rb, a, b, real_b, nstart, nend, o);
+    else if (WALK == WALK_HG) walk_reg_pair<RegHG>(ra, rb, a, b, real_b, nstart, nend, o);
+    else if (WALK == WALK_HGL) walk_reg_pair<RegHGL>(ra, rb, a, b, real_b, nstart, nend, o);
+    else if (WALK == WALK_HG96) walk_reg_pair<RegHG96>(ra, rb, a, b, real_b, nstart, nend, o);
     else if (WALK == WALK_H64) walk_reg_pair<RegH64>(ra, rb, a, b, real_b, nstart, nend, o);
     else if (WALK == WALK_H96) walk_reg_pair<RegH96>(ra, rb, a, b, real_b, nstart, nend, o);
     else if (WALK == WALK_H32) walk_reg_pair<RegH32>(ra, rb, a, b, real_b, nstart, nend, o);
@@ -577,6 +624,9 @@ __device__ __forceinline__ void walk_quad_as(u64 (&r)[4], Prime (&c)[4], u32 nre
                                              const WalkOut& o) {
     if (nstart >= nend) return;
     if (WALK == WALK_HF) walk_reg4<RegHF>(r, c, nreal, nstart, nend, o);
+    else if (WALK == WALK_HG) walk_reg4<RegHG>(r, c, nreal, nstart, nend, o);
+    else if (WALK == WALK_HGL) walk_reg4<RegHGL>(r, c, nreal, nstart, nend, o);
+    else if (WALK == WALK_HG96) walk_reg4<RegHG96>(r, c, nreal, nstart, nend, o);
     else if (WALK == WALK_H64) walk_reg4<RegH64>(r, c, nreal, nstart, nend, o);
     else if (WALK == WALK_H96) walk_reg4<RegH96>(r, c, nreal, nstart, nend, o);
     else if (WALK == WALK_H32) walk_reg4<RegH32>(r, c, nreal, nstart, nend, o);
@@ -597,6 +647,9 @@ __device__ __forceinline__ void walk_quad_rt(int walk, u64 (&r)[4], Prime (&c)[4
                                              const WalkOut& o) {
     switch (walk) {
         case WALK_HF: walk_quad_as<WALK_HF>(r, c, nreal, nstart, nend, o); break;
+        case WALK_HG: walk_quad_as<WALK_HG>(r, c, nreal, nstart, nend, o); break;
+        case WALK_HGL: walk_quad_as<WALK_HGL>(r, c, nreal, nstart, nend, o); break;
+        case WALK_HG96: walk_quad_as<WALK_HG96>(r, c, nreal, nstart, nend, o); break;
         case WALK_H64: walk_quad_as<WALK_H64>(r, c, nreal, nstart, nend, o); break;
         case WALK_H96: walk_quad_as<WALK_H96>(r, c, nreal, nstart, nend, o); break;
         case WALK_H32: walk_quad_as<WALK_H32>(r, c, nreal, nstart, nend, o); break;

@@ -93,17 +93,20 @@ def test_split_searches_pass_the_round_trip(ctx, orc, steps):
 # from stored residues and walked-n tags, and may take a different step as the
 # multipliers grow
 SPLIT_REGIMES = [
-    (10**15, 10**15 + 200_000, 100_000, 100_700),                  # half-offset 96-bit
+    (10**15, 10**15 + 200_000, 100_000, 100_700),                  # float quotient, 96-bit product
+    (10**15, 10**15 + 200_000, 1_276_000, 1_277_000),              # ... into the half-offset 96-bit step at its k_max bound
     (10**13, 10**13 + 30_000, 67_108_000, 67_109_700),             # half-offset 96-bit into lazy 96-bit at 2^26
     ((1 << 63) + 1, (1 << 63) + 200_000, 5_000, 5_700),             # half-offset canonical 96-bit
     ((1 << 63) + 1, (1 << 63) + 10_001, (1 << 26) - 300, (1 << 26) + 400),  # into canonical 96-bit at 2^26
     ((1 << 64) - 200_000, (1 << 64) - 1, 1_000, 1_333),              # near 2^64
-    (10**12, 10**12 + 200_000, 100_000, 100_700),                  # float quotient
-    (10**12, 10**12 + 200_000, 441_000, 442_000),                  # float quotient into the lazy 64-bit step
-    ((1 << 34) + 1, (1 << 34) + 200_001, 20_000, 20_900),          # shifted-window 64-bit
-    ((1 << 31) - 100_000, (1 << 31) + 100_000, 2000, 2900),         # 32-bit / shifted-window boundary
+    (10**12, 10**12 + 200_000, 100_000, 100_700),                  # float quotient, window from the least p
+    (10**12, 10**12 + 200_000, 441_000, 442_000),                  # ... into the k_max-aware window
+    (10**12, 10**12 + 200_000, 1_276_000, 1_277_000),              # ... into the half-offset lazy 64-bit step
+    ((1 << 34) + 1, (1 << 34) + 200_001, 20_000, 20_900),          # float quotient, window shift <= 32
+    ((1 << 34) + 1, (1 << 34) + 200_001, 1_276_000, 1_277_000),    # ... into the shifted-window step
+    ((1 << 31) - 100_000, (1 << 31) + 100_000, 2000, 2900),         # across 2^31: a step per candidate
     (10**9, 10**9 + 20_000, 67_108_000, 67_109_000),               # 32-bit step into the generic walk
-    ((1 << 33) - 100_000, (1 << 33) + 100_000, 2000, 2900),         # generic / lazy boundary
+    ((1 << 33) - 100_000, (1 << 33) + 100_000, 2000, 2900),         # float quotient across 2^33
     (1_000_000, 1_100_000, 1000, 3000),                            # small p, many hits
 ]
 

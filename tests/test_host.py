@@ -133,6 +133,7 @@ def test_context_needs_a_device(fslib):
 def test_walk_step_selection_boundaries(fslib):
     """The launch-wide step the host proves valid for a p-segment (fs_walk_step)."""
     H64, T64, L96, C96, H96, H32, HM, C96H, HF, ANY = 4, 1, 2, 3, 5, 6, 7, 8, 9, 0
+    HG, HGL, HG96 = 10, 11, 12
     ws = fslib.walk_step
     assert ws(10**12, 10**12 + 10**8, 200_000) == HF                       # config 2
     assert ws(10**12, 10**12 + 10**9, 200_000) == HF                       # config 2, whole range
@@ -141,26 +142,44 @@ def test_walk_step_selection_boundaries(fslib):
     assert ws(10**6, 2 * 10**6, 2000) == H32                               # config 1: p < 2^31
     assert ws(127, 100_000, 1_000_000) == H32                              # self test 3 (p <= nmax)
     assert ws((1 << 31) - 1000, (1 << 31) + 1000, 2000) == ANY              # straddles 2^31
-    assert ws((1 << 32) + 1, (1 << 32) + 1000, 2000) == HM                  # 2^31 <= p < 2^36: shifted window
+    assert ws((1 << 32) + 1, (1 << 32) + 1000, 2000) == HGL                 # 2^31 <= p, window s <= 32: float quotient
+    assert ws((1 << 32) + 1, (1 << 32) + 1000, 1_276_527) == HM             # ... k_max past 46 k_max < 7 2^23: shifted window
     assert ws((1 << 32) + 1, (1 << 32) + 1000, 1 << 25) == ANY              # ... with k_max >= 2^25: generic
     assert ws(10**6, 2 * 10**6, 1 << 26) == ANY                             # k_max >= 2^26 at small p
-    assert ws(1 << 36, (1 << 36) + 1000, 2000) == H64
-    assert ws((1 << 36) - 1000, (1 << 36) + 1000, 2000) == T64              # straddles 2^36: the step valid on both sides
+    assert ws(1 << 36, (1 << 36) + 1000, 2000) == HGL
+    assert ws((1 << 36) - 1000, (1 << 36) + 1000, 2000) == HGL              # no bound at 2^36 for the float quotient
+    assert ws(1 << 36, (1 << 36) + 1000, 1 << 21) == H64                    # k_max past the float quotient's bound
+    assert ws((1 << 36) - 1000, (1 << 36) + 1000, 1 << 21) == T64           # ... straddling 2^36: the step valid on both sides
     # float-quotient step: p >= 2^38, 19 kmax <= 2^23, 19 pmax kmax < 2^(bitlen(plo) + 23), p kmax <= 2^62
     assert ws(1 << 38, (1 << 38) + 1000, 2000) == HF
-    assert ws((1 << 38) - 1000, (1 << 38) + 1000, 2000) == H64             # straddles 2^38
+    assert ws((1 << 38) - 1000, (1 << 38) + 1000, 2000) == HGL             # straddles 2^38: window s = 26 on both sides
     assert ws(10**12, 10**12 + 30_000, 441_505) == HF                       # 19 kmax <= 2^23
-    assert ws(10**12, 10**12 + 30_000, 441_506) == H64
+    assert ws(10**12, 10**12 + 30_000, 441_506) == HG                       # k_max-aware window, s >= 32
     assert ws((1 << 39) + 1, (1 << 40) - 1, 441_505) == HF                  # 19 pmax kmax < 2^63
-    assert ws((1 << 39) - 1000, (1 << 40) - 1, 441_505) == H64              # bitlen(plo) 39: z could reach 2^23
+    assert ws((1 << 39) - 1000, (1 << 40) - 1, 441_505) == HG               # bitlen(plo) 39: z could reach 2^23 in HF's window
     assert ws((1 << 50) - 10_000, (1 << 50) + 1, 4096) == HF                # p kmax = 2^62 exactly
-    assert ws((1 << 50) - 10_000, (1 << 50) + 2, 4096) == H96               # just above
+    assert ws((1 << 50) - 10_000, (1 << 50) + 2, 4096) == HG                # just above: t < 23/16 p k_max < 2^64 still
     assert ws((1 << 35) + 1, (1 << 35) + 1000, 1 << 25) == T64              # 2^33 < p < 2^36, k_max >= 2^25
     k = 1 << 20
-    assert ws(1 << 40, (1 << 40) + 1, k) == H64                             # p kmax = 2^60
-    assert ws((1 << 42) - 10, (1 << 42) + 1, k) == H64                      # p kmax = 2^62 exactly
-    assert ws((1 << 42) - 10, (1 << 42) + 2, k) == H96                      # just above: 96-bit, half-offset
-    assert ws(10**13, 10**13 + 30_000, (1 << 26) - 1) == H96
+    assert ws(1 << 40, (1 << 40) + 1, k) == HG                              # p kmax = 2^60
+    assert ws((1 << 42) - 10, (1 << 42) + 1, k) == HG                       # p kmax = 2^62 exactly
+    assert ws((1 << 44) + 1, (1 << 44) + 1000, k) == HG96                   # 23/16 p k_max >= 2^64: 96-bit t
+    assert ws((1 << 42) - 10, (1 << 42) + 2, 1 << 21) == H96                # k_max past the bound: 96-bit, half-offset
+    # HG needs 23/16 pmax k_max < 2^64 (t in 64 bits), HG96 p < 2^63 and s < 64
+    kb = 1_276_526
+    edge = ((1 << 68) - 1) // (23 * kb)                                     # last pmax with ceil(23 pmax kb / 16) < 2^64
+    assert ws(edge - 1000, edge + 1, kb) == HG and ws(edge - 1000, edge + 2, kb) == HG96
+    assert ws((1 << 63) - 10**6, (1 << 63) - 1, kb) == HG96 and ws((1 << 63) - 10**6, 1 << 63, kb) == HG96
+    assert ws(1 << 63, (1 << 63) + 10**6, 1000) == C96H                     # p >= 2^63: no float-quotient step
+    # the window shift on one side of 32: HGL while T = ceil(23 pmax k_max / 16) < 2^56
+    # (s <= 32), HG while T(plo) >= 2^55 (s >= 32), neither across both
+    T = lambda p: (23 * p * kb + 15) // 16
+    last56, first55 = 39_268_312_544, 19_634_156_273
+    assert T(last56) < 1 << 56 <= T(last56 + 1) and T(first55 - 1) < 1 << 55 <= T(first55)
+    assert ws(last56 - 1000, last56 + 1, kb) == HGL and ws(last56 - 1000, last56 + 2, kb) == HG
+    assert ws(first55, last56 + 10**6, kb) == HG
+    assert ws(first55 - 1, last56 + 10**6, kb) == HM                       # s from 31 to 33: shifted window
+    assert ws(10**13, 10**13 + 30_000, (1 << 26) - 1) == H96                # k_max past the float quotient's bound
     assert ws(10**13, 10**13 + 30_000, 1 << 26) == L96
     assert ws(10**13, 10**13 + 30_000, 1 << 28) == ANY                      # k_max >= 2^28: generic
     assert ws((1 << 63) - 1000, (1 << 63) + 1000, 5000) == ANY              # straddles 2^63
@@ -258,6 +277,81 @@ def test_float_quotient_window_holds_where_the_host_selects_it(fslib):
                 assert r2 % p == (r * k) % p
                 assert 16 * r2 < 19 * p
                 r = r2
+
+
+def _halfg_step(r, k, p, kmax, form):
+    """Word-level restatement of the float-quotient steps with a k_max-aware
+    window (make_halfg, fs_arith.cuh): s = bitlen(ceil(23 p kmax / 16)) - 24,
+    z = floor(t / 2^s) read as the subnormal z 2^-149 (24 bits at most), one
+    fma by m 2^(s-e) rounding down on the subnormal grid.  form: 10 HG, 11 HGL,
+    12 HG96 (fs_walk_step's values)."""
+    from fractions import Fraction
+    T = (23 * p * kmax + 15) // 16
+    s = T.bit_length() - 24
+    assert (s >= 32) if form in (10, 12) else (s <= 32)
+    bl = p.bit_length()
+    e = bl + 23
+    m = (1 << e) // p
+    assert (1 << 23) <= m < (1 << 24)
+    g = _f32(((s - e + 149) << 23) + m)
+    assert g == Fraction(m, 1 << (e - s))
+    t = r * k
+    assert t < (1 << 64) if form in (10, 11) else t < (1 << 96)
+    z = t >> s
+    assert z < 1 << 24
+    assert _f32(z) == Fraction(z, 1 << 149)                  # exponent field 0 or 1: spacing 2^-149
+    prod = _f32(z) * g
+    assert prod < Fraction(1, 1 << 125)
+    q = int(prod * (1 << 149))
+    assert q <= t // p
+    return (t + q * ((1 << 64) - p)) % (1 << 64)
+
+
+def test_kmax_window_float_quotient_holds_where_the_host_selects_it(fslib):
+    """Wherever fs_walk_step picks one of the float-quotient steps with a
+    k_max-aware window (10, 11, 12), each step is exact and keeps r below
+    (23/16) p < x + p, for the least and largest p of the range over the last
+    multipliers up to k_max, k_max up to the bound 46 k_max < 7 2^23."""
+    import random
+    rng = random.Random(5)
+    seen = {10: 0, 11: 0, 12: 0}
+    tries = 0
+    while min(seen.values()) < 12:
+        tries += 1
+        assert tries < 200_000
+        bits = rng.randrange(31, 63)
+        lo = rng.randrange(1 << bits, 1 << (bits + 1))
+        if lo >= 1 << 63:
+            continue
+        w = rng.choice([1000, 10**6, 1 << max(bits - 8, 10)])
+        kmax = rng.choice([rng.randrange(441_506, 1_276_527), 1_276_526, rng.randrange(2, 441_506)])
+        step = fslib.walk_step(lo, lo + w, kmax)
+        if step not in seen:
+            continue
+        seen[step] += 1
+        for p in (lo | 1, (lo + w - 1) | 1):
+            if p >= lo + w:
+                p -= 2
+            r = p - 1
+            for k in range(max(1, kmax - 120), kmax + 1):
+                r2 = _halfg_step(r, k, p, kmax, step)
+                assert r2 % p == (r * k) % p
+                assert 16 * r2 < 23 * p
+                r = r2
+    # the corners: p just below 2^63 with k_max at the bound (96-bit t), and
+    # the window shift on both sides of 32
+    for lo, hi, kmax, want in [((1 << 63) - 10_001, (1 << 63) - 1, 1_276_526, 12),
+                               ((1 << 31) + 1, (1 << 31) + 1001, 1_276_526, 11),
+                               ((1 << 40) + 1, (1 << 40) + 1001, 1_276_526, 10)]:
+        assert fslib.walk_step(lo, hi, kmax) == want
+        p = (hi - 2) | 1
+        r = p - 1
+        for k in range(kmax - 200, kmax + 1):
+            r2 = _halfg_step(r, k, p, kmax, want)
+            assert r2 % p == (r * k) % p and 16 * r2 < 23 * p
+            r = r2
+    # beyond the k_max bound the steps are not chosen
+    assert fslib.walk_step((1 << 40) + 1, (1 << 40) + 1001, 1_276_527) not in (10, 11, 12)
 
 
 def _pm_mul(a, b, p):
