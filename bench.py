@@ -195,7 +195,7 @@ def roofline(ctx, fs, wl, ncand, st, step_ms, clocks=None, seg=None, segments=1)
         "setup_products_per_candidate": smp,
         "setup_product": "folding modulo 2^63 + d" if folded else "Montgomery",
         "peak_source": "measured on this GPU: the walk step's PTX block and mont_mul, register-resident at full "
-                       "occupancy (fs_bench_int_pipe kinds 4-15)",
+                       "occupancy (fs_bench_int_pipe kinds 4-18)",
         "imad_pipe_busy_ncu": cap.get("imad_pipe_busy"), "ncu_source": cap.get("source"),
         "hbm": {"achieved": hbm_ach, "peak": hbm_peak, "unit": "GB/s",
                 "frac": hbm_ach / hbm_peak if hbm_peak else None,
