@@ -11,7 +11,9 @@
 //   primes per thread        sieve_variant 3 (two) or 5 (four)
 //   blocks per SM            sieve_blocks_per_sm: 1x, 2x, 4x the resident ones
 //   threads per block        sieve_block_threads: 256 or 128
-//   n-steps per launch       max_steps_per_launch: the whole n-range, or halves
+//   n-steps per launch       max_steps_per_launch: the whole n-range, all but
+//                            the last 8 steps (the check in a launch of its
+//                            own), or halves
 // keeps the fastest (a shape must beat the one before by 0.5 % to replace it,
 // so noise does not move the choice), applies it to the context, and sizes
 // the segment so one launch takes about target_ms at the measured rate.
@@ -50,6 +52,19 @@ std::string gpu_name(fs_ctx* c) {
 
 int lg(double x) { return (int)std::floor(std::log2(std::max(x, 1.0))); }
 
+uint32_t steps_code(uint32_t steps, uint32_t W) {
+    if (steps == 0 || steps >= W) return 0;
+    if (W > 8 && steps == W - 8) return 1;
+    if (steps == (W + 1) / 2) return 2;
+    return steps > 2 ? steps : 0;
+}
+
+uint32_t steps_from_code(uint32_t code, uint32_t W) {
+    if (code == 1) return W > 8 ? W - 8 : 0;
+    if (code == 2) return (W + 1) / 2;
+    return code;
+}
+
 std::string search_key(fs_ctx* c, uint64_t pmin, uint32_t nmin, uint32_t nmax) {
     char buf[256];
     snprintf(buf, sizeof buf, "search|%s|sm%d|W%d|P%d|N%d", gpu_name(c).c_str(), c->sm_count,
@@ -57,7 +72,9 @@ std::string search_key(fs_ctx* c, uint64_t pmin, uint32_t nmin, uint32_t nmax) {
     return buf;
 }
 
-// One cached choice: a text line "<key> <variant> <bpsm> <threads> <steps> <tile> <rate>".
+// One cached choice: a text line "<key> <variant> <bpsm> <threads> <steps> <tile> <rate>",
+// <steps> coded against the search's own n-width W (the bucket holds several):
+// 0 one launch, 1 all but the last 8 steps, 2 halves (larger: that many steps).
 struct Entry {
     uint32_t variant = 0, bpsm = 0, threads = 0, steps = 0, tile = 0;
     double rate = 0;
@@ -212,7 +229,7 @@ extern "C" int fs_autotune(fs_ctx* c, uint64_t pmin, uint64_t pmax, uint32_t nmi
         t.sieve_variant = e.variant;
         t.sieve_blocks_per_sm = e.bpsm;
         t.sieve_block_threads = e.threads;
-        t.max_steps_per_launch = e.steps;
+        t.max_steps_per_launch = steps_from_code(e.steps, nmax - nmin);
         t.batch_tile_candidates = c->tuning.batch_tile_candidates;
         if ((rc = fs_set_tuning(c, &t))) return rc;
         fill_result(c, pmin, pmax, nmin, nmax, target_ms, e.rate, out);
@@ -282,10 +299,16 @@ extern "C" int fs_autotune(fs_ctx* c, uint64_t pmin, uint64_t pmax, uint32_t nmi
         rc = consider(t);
     }
     if (!rc && W >= 4096) {
-        // the n-range in two launches instead of one
-        fs_tuning t = best;
-        t.max_steps_per_launch = (W + 1) / 2;
-        rc = consider(t);
+        // the n-range in two launches instead of one: all but the last eight
+        // steps in a launch that stores residues and tags, and the final check
+        // in a launch of its own (the walk loop of a kernel that also checks
+        // runs 1-2 % slower for some steps and faster for others), or halves
+        const fs_tuning base = best;
+        for (uint32_t steps : {W - 8, (W + 1) / 2}) {
+            fs_tuning t = base;
+            t.max_steps_per_launch = steps;
+            if ((rc = consider(t))) break;
+        }
     }
     c->active = false;   // the sample searches are over; the caller begins its own
     restore_stats(c, saved);
@@ -301,7 +324,7 @@ extern "C" int fs_autotune(fs_ctx* c, uint64_t pmin, uint64_t pmax, uint32_t nmi
     ne.variant = best.sieve_variant;
     ne.bpsm = best.sieve_blocks_per_sm;
     ne.threads = best.sieve_block_threads;
-    ne.steps = best.max_steps_per_launch;
+    ne.steps = steps_code(best.max_steps_per_launch, W);
     ne.rate = best_rate;
     cache_put(cache_path, key, ne);
     return FS_OK;

@@ -717,13 +717,29 @@ __global__ void __launch_bounds__(kSieveThreads, MINB) sieve_kernel(SieveArgs a)
     __shared__ HitStage st;
     __shared__ u64 wsum[kSieveThreads / 32];
     __shared__ u32 wbad[kSieveThreads / 32];
+    // With the float-quotient steps, each thread's checksum and validation
+    // count stay in shared memory across the walk (volatile: not promoted to
+    // registers), so that the walk loop of a checking kernel is allocated like
+    // a storing one's: in registers they cost config 2's fused launch 1.2 %
+    // and a 96-bit float-quotient launch 1.5 %.  The 96-bit steps for
+    // p >= 2^63 keep them in registers (shared costs config 3 2.9 %).
+    constexpr bool kAccShared = FINAL && PPT == 4 &&
+                                (WALK == WALK_HF || WALK == WALK_HG || WALK == WALK_HGL || WALK == WALK_HG96);
+    __shared__ u64 tsum_[kAccShared ? kSieveThreads : 1];
+    __shared__ u32 tbad_[kAccShared ? kSieveThreads : 1];
+    volatile u64* tsum = tsum_;
+    volatile u32* tbad = tbad_;
+    if (kAccShared) {
+        tsum[threadIdx.x] = 0;
+        tbad[threadIdx.x] = 0;
+    }
+    u64 sum = 0;
+    u32 bad = 0;
     if (threadIdx.x == 0) st.n = 0;
     __syncthreads();
     const u32 ncand = *a.ncand;
     const u32 n = ncand < a.cap ? ncand : a.cap;
     const WalkOut o{&st, a.hits, a.hitcap, a.ctr, 0};
-    u64 sum = 0;
-    u32 bad = 0;
     // every residue of the launch advances by the launch's steps
     const u32 steps = a.nend > a.nstart ? a.nend - a.nstart : 0;
     const u32 stride = gridDim.x * blockDim.x;
@@ -754,16 +770,25 @@ __global__ void __launch_bounds__(kSieveThreads, MINB) sieve_kernel(SieveArgs a)
                 for (int h = 1; h < 4; ++h) r[h] = (u32)h < nreal ? start_residue_one<SETUP>(a, c[h], i0 + h) : r[0];
             }
             walk_quad_as<WALK>(r, c, nreal, a.nstart, a.nend, o);
+            u64 qsum = 0;
+            u32 qbad = 0;
 #pragma unroll
             for (int h = 0; h < 4; ++h) {
                 if ((u32)h >= nreal) break;
                 const u32 nw = start_n<SETUP>(a, i0 + h) + steps;
                 if (FINAL) {
-                    final_check(c[h], r[h], nw, a.nmax, sum, bad);
+                    final_check(c[h], r[h], nw, a.nmax, qsum, qbad);
                 } else {
                     a.residue[i0 + h] = r[h];
                     if (a.walked) a.walked[i0 + h] = nw;
                 }
+            }
+            if (kAccShared) {
+                tsum[threadIdx.x] = tsum[threadIdx.x] + qsum;
+                tbad[threadIdx.x] = tbad[threadIdx.x] + qbad;
+            } else if (FINAL) {
+                sum += qsum;
+                bad += qbad;
             }
         }
     } else {
@@ -800,6 +825,10 @@ __global__ void __launch_bounds__(kSieveThreads, MINB) sieve_kernel(SieveArgs a)
     }
     }
     if (FINAL) {
+        if (kAccShared) {
+            sum = tsum[threadIdx.x];
+            bad = tbad[threadIdx.x];
+        }
         // warp then block reduction of the checksum, one atomic per block
 #pragma unroll
         for (int d = 16; d; d >>= 1) {

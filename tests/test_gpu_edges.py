@@ -116,16 +116,21 @@ def test_plan_check_flags_a_corrupted_plan(ctx, what):
 
 
 def test_ceiling_kernels_report_rates(ctx):
-    """The roofline's ceiling microkernels (fs_bench_int_pipe kinds 0-15) run and
-    report plausible rates; an unknown kind is refused."""
+    """The roofline's ceiling microkernels (fs_bench_int_pipe kinds 0-18) run and
+    report plausible rates; an unknown kind is refused, and so are iterations
+    that would take the k_max-window float-quotient kinds (16-18) past their
+    multiplier bound."""
     import factsieve_gb300 as fs
-    rates = {k: ctx.bench_int_pipe(k, 200)[0] for k in range(16)}
+    rates = {k: ctx.bench_int_pipe(k, 200)[0] for k in range(19)}
     assert all(v > 0 for v in rates.values()), rates
     assert rates[0] > rates[4]             # an IMAD issues faster than a Montgomery product completes
     with pytest.raises(fs.FSError):
-        ctx.bench_int_pipe(16, 200)
+        ctx.bench_int_pipe(19, 200)
     with pytest.raises(fs.FSError):
         ctx.bench_int_pipe(5, 0)
+    ctx.bench_int_pipe(17, 147_065)        # multipliers up to 100,001 + 8 x 147,065 = 1,276,521
+    with pytest.raises(fs.FSError):
+        ctx.bench_int_pipe(17, 147_066)
 
 
 def test_pending_count_sizes_collect(ctx, orc):

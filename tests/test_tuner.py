@@ -24,13 +24,19 @@ def test_tuned_search_gives_identical_results_and_is_cached(ctx, tmp_path):
         assert t["sieve_variant"] in (3, 5) and t["sieve_block_threads"] in (128, 256)
         assert ctx.tuning()["sieve_variant"] == t["sieve_variant"]        # applied to the context
         assert 1e5 <= best["seg_width"] <= 4_294_900_000
-        assert best["steps_per_launch"] in (100_000, 50_000)
+        assert best["steps_per_launch"] in (100_000, 99_992, 50_000)       # one launch, the check apart, halves
         tuned = ctx.sieve(*CHECK, seg_width=best["seg_width"])
         assert (tuned.raw_sum, tuned.primecount, tuned.checksum) == (base.raw_sum, base.primecount, base.checksum)
         # the same bucket again: read from the cache, nothing timed
         again = tuner.autotune(ctx, 10**12 + 7, 10**12 + 4 * 10**10, 100_003, 200_003, cache_path=cache)
         assert again["from_cache"] == 1 and again["shapes_tried"] == 0
         assert again["tuning"] == best["tuning"]
+        # the split is cached against the n-width: the same choice for a
+        # narrower n-range of the bucket
+        other = tuner.autotune(ctx, 10**12 + 7, 10**12 + 4 * 10**10, 100_000, 190_000, cache_path=cache)
+        assert other["from_cache"] == 1
+        split = {100_000: 0, 99_992: 89_992, 50_000: 45_000}[best["steps_per_launch"]]
+        assert other["tuning"]["max_steps_per_launch"] == split
         lines = open(cache).read().splitlines()
         assert len(lines) == 1 and lines[0].startswith("search|")
     finally:
@@ -52,6 +58,7 @@ def test_a_short_run_keeps_the_defaults(ctx, tmp_path):
     dict(sieve_variant=3, sieve_blocks_per_sm=6, sieve_block_threads=128),
     dict(sieve_variant=5, sieve_blocks_per_sm=16, sieve_block_threads=128),
     dict(sieve_variant=5, sieve_blocks_per_sm=2, sieve_block_threads=256, max_steps_per_launch=333),
+    dict(sieve_variant=5, max_steps_per_launch=992),                  # the check in a launch of its own
 ])
 def test_every_shape_the_tuner_tries_gives_identical_results(ctx, orc, shape):
     lo, hi, nmin, nmax = 10**12, 10**12 + 3_000_000, 100_000, 101_000
