@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 
 namespace fs {
 
@@ -42,6 +43,21 @@ std::vector<uint32_t> primes_upto(uint32_t n) {
     return out;
 }
 
+// The primes up to n from one list kept for the process (grown when a larger
+// n comes): the setup plan of every search, batch job and served job starts
+// from it, and sieving again each time was a third of a plan's host time.
+std::vector<uint32_t> primes_upto_cached(uint32_t n) {
+    static std::mutex mu;
+    static std::vector<uint32_t> list;
+    static uint32_t upto = 0;
+    std::lock_guard<std::mutex> lock(mu);
+    if (n > upto) {
+        list = primes_upto(n);
+        upto = n;
+    }
+    return std::vector<uint32_t>(list.begin(), std::upper_bound(list.begin(), list.end(), n));
+}
+
 uint32_t legendre(uint32_t q, uint32_t n) {
     uint32_t e = 0;
     for (uint64_t qk = q; qk <= n; qk *= q) e += (uint32_t)(n / qk);
@@ -50,7 +66,7 @@ uint32_t legendre(uint32_t q, uint32_t n) {
 
 RefTable reference_table(uint32_t n) {
     RefTable t;
-    std::vector<uint32_t> pr = primes_upto(n);
+    const std::vector<uint32_t> pr = primes_upto_cached(n);
     size_t i = 0;
     while (i < pr.size()) {
         uint32_t e = legendre(pr[i], n);
@@ -82,8 +98,24 @@ RefTable reference_table(uint32_t n) {
 // links point from a taken slot to the next one below it.
 static void pack_layer(const std::vector<uint32_t>& v, std::vector<uint64_t>& words) {
     const uint32_t m = (uint32_t)v.size();
+    if (m == 0) return;
     std::vector<uint32_t> below(m + 1);   // slot i + 1 holds v[i]; 0: none left
     for (uint32_t i = 0; i <= m; ++i) below[i] = i;
+    // slots holding primes <= x, for the common cases without a search: x at
+    // least the largest prime (a word's second and third prime, as a rule)
+    // and x below 4096 (the small prime that fills a word's hole)
+    constexpr uint32_t kSmall = 4096;
+    std::vector<uint32_t> upto(kSmall);
+    for (uint32_t x = 0, i = 0; x < kSmall; ++x) {
+        while (i < m && v[i] <= x) ++i;
+        upto[x] = i;
+    }
+    const uint64_t vmax = v[m - 1];
+    auto slots_upto = [&](uint64_t x) -> uint32_t {
+        if (x >= vmax) return m;
+        if (x < kSmall) return upto[x];
+        return (uint32_t)(std::upper_bound(v.begin(), v.end(), x) - v.begin());
+    };
     auto find = [&below](uint32_t x) {
         while (below[x] != x) {
             below[x] = below[below[x]];
@@ -95,9 +127,7 @@ static void pack_layer(const std::vector<uint32_t>& v, std::vector<uint64_t>& wo
         uint64_t w = v[top - 1];
         below[top] = top - 1;
         for (;;) {
-            const uint64_t lim = UINT64_MAX / w;
-            const uint32_t k = (uint32_t)(std::upper_bound(v.begin(), v.end(), lim) - v.begin());
-            const uint32_t s = find(k);
+            const uint32_t s = find(slots_upto(UINT64_MAX / w));
             if (s == 0) break;
             w *= v[s - 1];
             below[s] = s - 1;
@@ -109,7 +139,7 @@ static void pack_layer(const std::vector<uint32_t>& v, std::vector<uint64_t>& wo
 SetupPlan build_plan(uint32_t n, uint32_t chunks) {
     SetupPlan plan;
     plan.n = n;
-    std::vector<uint32_t> pr = primes_upto(n);
+    const std::vector<uint32_t> pr = primes_upto_cached(n);
     plan.nprimes = pr.size();
     const uint32_t e2 = n >= 2 ? legendre(2, n) : 0;
     // odd primes and their exponents
@@ -122,16 +152,16 @@ SetupPlan build_plan(uint32_t n, uint32_t chunks) {
             e.push_back(legendre(x, n));
         }
     if (chunks < 1) chunks = 1;
-    // balance chunks by bit mass sum(log2 q * popcount(e))
-    std::vector<double> mass(q.size());
-    double total = 0;
-    for (size_t i = 0; i < q.size(); ++i) {
-        mass[i] = std::log2((double)q[i]) * __builtin_popcount(e[i]);
-        total += mass[i];
-    }
     std::vector<size_t> cut(chunks + 1, q.size());
     cut[0] = 0;
-    {
+    if (chunks > 1) {
+        // balance chunks by bit mass sum(log2 q * popcount(e))
+        std::vector<double> mass(q.size());
+        double total = 0;
+        for (size_t i = 0; i < q.size(); ++i) {
+            mass[i] = std::log2((double)q[i]) * __builtin_popcount(e[i]);
+            total += mass[i];
+        }
         double acc = 0;
         uint32_t c = 1;
         for (size_t i = 0; i < q.size() && c < chunks; ++i) {
@@ -147,15 +177,16 @@ SetupPlan build_plan(uint32_t n, uint32_t chunks) {
         uint32_t emax = (c == 0) ? e2 : 0;
         for (size_t i = cut[c]; i < cut[c + 1]; ++i) emax = std::max(emax, e[i]);
         int nbits = emax ? 32 - __builtin_clz(emax) : 0;
+        // each layer's primes, ascending: one pass over the chunk's primes
+        std::vector<std::vector<uint32_t>> lq(nbits);
+        for (size_t i = cut[c]; i < cut[c + 1]; ++i)
+            for (uint32_t x = e[i]; x; x &= x - 1) lq[__builtin_ctz(x)].push_back(q[i]);
         for (int b = nbits - 1; b >= 0; --b) {
             PlanLayer L;
             L.begin = (uint32_t)plan.words.size();
             L.dbl = (c == 0 && ((e2 >> b) & 1)) ? 1u : 0u;
             L.pad = 0;
-            std::vector<uint32_t> lq;
-            for (size_t i = cut[c]; i < cut[c + 1]; ++i)
-                if ((e[i] >> b) & 1) lq.push_back(q[i]);
-            pack_layer(lq, plan.words);
+            pack_layer(lq[b], plan.words);
             L.end = (uint32_t)plan.words.size();
             // Horner: the first layer of a chunk starts from 1 (no squaring)
             if (b != nbits - 1) ch.deficit *= 2;

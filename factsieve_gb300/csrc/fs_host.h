@@ -9,6 +9,7 @@ namespace fs {
 // for primesieve_generate_primes(2, nmin) (cl_sieve.cpp:797); the library's
 // source is not part of the reference tree.
 std::vector<uint32_t> primes_upto(uint32_t n);
+std::vector<uint32_t> primes_upto_cached(uint32_t n);
 
 // Legendre exponent of prime q in n!.
 uint32_t legendre(uint32_t q, uint32_t n);
