@@ -66,11 +66,11 @@ IMAD_PER_PRODUCT = 20   # reference m_mul on 32-bit limbs (8 mul_wide + 4 + 8)
 # busy share, from one `ncu --set full --clock-control none` capture of the
 # fused sieve kernel on the same workload (dram__bytes_read.sum +
 # dram__bytes_write.sum; sm__pipe_fmaheavy_cycles_active): config 2 captured
-# on a 1e8-wide segment (29,084,928 B) and scaled by 10 to the whole-range
+# on a 1e8-wide segment (29,087,744 B) and scaled by 10 to the whole-range
 # launch the bench times, config 3 on one of its 1e8-wide launches.
 NCU_CAPTURE = {   # workload -> sieve launches per segment -> capture
-    "config2": {1: {"traffic": 290_849_280, "imad_pipe_busy": 0.782,
-                    "source": "ncu --set full capture of sieve_kernel, bench.py --segment 1e8"},
+    "config2": {1: {"traffic": 290_877_440, "imad_pipe_busy": 0.785,
+                    "source": "ncu --set full capture of sieve_kernel, bench.py --segment 1e8 --max-steps 0"},
                 # the n-range in two launches: both launches of one 1e8-wide segment
                 # (29,672,960 and 73,291,520 B), averaged and scaled by 10; the first
                 # launch's 43 MB of residue state was still in L2 when it ended
