@@ -77,7 +77,7 @@ NCU_CAPTURE = {   # workload -> sieve launches per segment -> capture
                 2: {"traffic": 514_822_400, "imad_pipe_busy": 0.783,
                     "source": "ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum of both sieve_kernel "
                               "launches, bench.py --segment 1e8 --max-steps 50000"}},
-    "config3": {1: {"traffic": 18_765_568, "imad_pipe_busy": 0.836,
+    "config3": {1: {"traffic": 18_705_664, "imad_pipe_busy": 0.851,
                     "source": "ncu --set full capture of sieve_kernel, bench.py --workload config3"}},
 }
 GOLDEN = os.path.join(ROOT, "tests", "golden")
