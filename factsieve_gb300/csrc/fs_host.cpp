@@ -46,7 +46,10 @@ std::vector<uint32_t> primes_upto(uint32_t n) {
 // The primes up to n from one list kept for the process (grown when a larger
 // n comes): the setup plan of every search, batch job and served job starts
 // from it, and sieving again each time was a third of a plan's host time.
+// Above n = 2^27 (7.4 million primes, 30 MB) nothing is kept.
 std::vector<uint32_t> primes_upto_cached(uint32_t n) {
+    constexpr uint32_t kKeepUpto = 1u << 27;
+    if (n > kKeepUpto) return primes_upto(n);
     static std::mutex mu;
     static std::vector<uint32_t> list;
     static uint32_t upto = 0;
