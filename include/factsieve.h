@@ -337,7 +337,12 @@ int fs_setup_form(uint64_t plo, uint64_t phi);
 int fs_power_table(uint32_t n, uint64_t *prime, uint32_t *exp, uint32_t *bit, uint32_t cap,
                    uint32_t *len);
 /* The bit-layered setup plan the GPU uses for n!: words, layers as
- * {begin, end, dbl, 0} quadruples, total R-deficit. */
+ * {begin, end, dbl, 0} quadruples (from the top exponent bit down), total
+ * R-deficit.  Layer b's words multiply to the odd primes whose Legendre
+ * exponent has bit b set, packed best fit decreasing (each word starts from
+ * the largest prime left and takes the largest that still fits below 2^64);
+ * the setup squares between layers and doubles where bit b of the exponent
+ * of 2 is set. */
 int fs_setup_plan(uint32_t n, uint32_t chunks, uint64_t *words, uint64_t wcap, uint64_t *nwords,
                   uint32_t *layers4, uint32_t lcap, uint32_t *nlayers, uint64_t *deficit);
 /* Chunk boundaries of the same plan: chunk c owns layers
