@@ -104,6 +104,7 @@ STEP_CEILING_KIND = {6: (11, "32-bit half-offset step"), 7: (12, "shifted-window
                      10: (16, "half-offset 64-bit step, FP32 quotient over a k_max-sized window, s >= 32"),
                      11: (17, "half-offset 64-bit step, FP32 quotient over a k_max-sized window, s <= 32"),
                      12: (18, "half-offset 96-bit step, FP32 quotient over a k_max-sized window"),
+                     13: (19, "half-offset canonical 96-bit step, FP32 quotient over a k_max-sized window"),
                      4: (5, "half-offset lazy 64-bit step"),
                      5: (10, "half-offset lazy 96-bit step"), 8: (13, "half-offset canonical 96-bit step"),
                      1: (6, "lazy 64-bit step"),
@@ -145,7 +146,7 @@ def roofline(ctx, fs, wl, ncand, st, step_ms, clocks=None, seg=None, segments=1)
     walk_ceil, _ = ctx.bench_int_pipe(kind, 4000)
     mm_ceil, _ = ctx.bench_int_pipe(4, 4000)
     imad_ops, _ = ctx.bench_int_pipe(0, 20000)
-    folded = bool(fs.setup_form(pmin, min(pmin + seg, pmax))) and step in (3, 8)
+    folded = bool(fs.setup_form(pmin, min(pmin + seg, pmax))) and step in (3, 8, 13)
     # the folding product's own ceiling is below Montgomery's at full occupancy
     # (it wins inside the fused kernel, at 2 blocks per SM): the peak takes the
     # faster of the two, so it never rests on the slower form
@@ -195,7 +196,7 @@ def roofline(ctx, fs, wl, ncand, st, step_ms, clocks=None, seg=None, segments=1)
         "setup_products_per_candidate": smp,
         "setup_product": "folding modulo 2^63 + d" if folded else "Montgomery",
         "peak_source": "measured on this GPU: the walk step's PTX block and mont_mul, register-resident at full "
-                       "occupancy (fs_bench_int_pipe kinds 4-18)",
+                       "occupancy (fs_bench_int_pipe kinds 4-19)",
         "imad_pipe_busy_ncu": cap.get("imad_pipe_busy"), "ncu_source": cap.get("source"),
         "hbm": {"achieved": hbm_ach, "peak": hbm_peak, "unit": "GB/s",
                 "frac": hbm_ach / hbm_peak if hbm_peak else None,

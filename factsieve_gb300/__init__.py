@@ -209,8 +209,9 @@ def walk_step(plo: int, phi: int, kmax: int) -> int:
     (6 / 7 / 9 / 4 / 5 / 8 half-offset 32-bit / shifted-window 64-bit / 64-bit
     with the quotient on the FP32 pipe / lazy 64-bit / lazy 96-bit / canonical
     96-bit; 10 / 11 / 12 half-offset with the FP32 quotient over a window sized
-    from kmax, s >= 32 / s <= 32 / 96-bit product; 1 lazy 64-bit, 2 lazy 96-bit,
-    3 canonical 96-bit, 0 chosen per candidate)."""
+    from kmax, s >= 32 / s <= 32 / 96-bit product; 13 the same quotient in the
+    half-offset canonical 96-bit step for p >= 2^63; 1 lazy 64-bit, 2 lazy
+    96-bit, 3 canonical 96-bit, 0 chosen per candidate)."""
     return int(lib().fs_walk_step(plo, phi, kmax))
 
 

@@ -1145,4 +1145,122 @@ __device__ __forceinline__ u32 canon96h_walk8x2(u32& al, u32& ah, u32& bl, u32& 
     return flag;
 }
 
+// ----- iterate: 96-bit steps for p >= 2^63, half-offset form, float quotient --
+//
+// canon96h_walk8x2 with its quotient taken as in make_halfg instead of by
+// IMAD.HI: for each candidate, T = ceil(23 p k_max / 16) and the window
+// shift s = bitlen(T) - 24 (40 to 64 for p >= 2^63), z = floor(t / 2^s) <
+// 2^24 read as the float z 2^-149, and q = floor(z g) from one round-down FMA
+// by g = m 2^(s-e), m = floor(2^e / p), e = bitlen(p) + 23 = 87.  The estimate
+// never exceeds t/p and falls short of it by less than 1 + (46/16) k_max
+// 2^-23, so for 46 k_max < 7 2^23 a residue below (23/16) p stays below it:
+// 65 bits inside the block (the 65th in a register, as in canon96h_walk8x2),
+// folded to [0, p) at the end of the block.  The hit test is the half-offset
+// one on canonical residues, r in {x, x + 1}; (23/16) p < x + p keeps the
+// lifted values out of reach.
+struct Canon96G {
+    u64 p, x;
+    u32 p0, p1;               // p (two words)
+    float g;                  // m 2^(s - e)
+    u32 sh;                   // s - 32
+    u32 x0, x1;               // low words of x and x + 1
+};
+
+__device__ __forceinline__ bool canon96g_ok(u64 p, u32 kmax) {
+    return (p >> 63) != 0 && kmax != 0 && kmax <= kHalfGMaxK;
+}
+
+__device__ __forceinline__ Canon96G make_canon96g(const Prime& c, u32 kmax) {
+    Canon96G C;
+    C.p = c.p;
+    C.x = (c.p - 1) >> 1;
+    C.p0 = (u32)c.p;
+    C.p1 = (u32)(c.p >> 32);
+    const int e = 64 + 23, s = halfg_window(c.p, kmax);
+    C.g = __uint_as_float(((u32)(s - e + 149) << 23) + recip_pow2(c.p, e));
+    C.sh = (u32)(s - 32);
+    C.x0 = (u32)C.x;
+    C.x1 = (u32)(C.x + 1);
+    return C;
+}
+
+// floor(z g) for a window z < 2^24 (the subnormal construction of halfg_quot).
+__device__ __forceinline__ u32 fquot(u32 z, float g) {
+    u32 q;
+    asm("{\n\t"
+        ".reg .f32 f;\n\t"
+        "mov.b32 f, %1;\n\t"
+        "fma.rm.f32 f, f, %2, 0f00000000;\n\t"
+        "mov.b32 %0, f;\n\t"
+        "}"
+        : "=r"(q)
+        : "r"(z), "f"(g));
+    return q;
+}
+
+// One step with the fold (canonical in and out): the replay and tail steps.
+__device__ __forceinline__ u64 canon96g_step(u64 r, u32 k, const Canon96G& C) {
+    const u64 lo = r * (u64)k, hi = __umul64hi(r, (u64)k);
+    const u32 q = fquot(top_bits(lo, hi, C.sh), C.g);
+    const u64 qlo = (u64)q * C.p, qhi = __umul64hi((u64)q, C.p);
+    const u64 rl = lo - qlo;
+    const u64 r2 = hi - qhi - (lo < qlo ? 1ull : 0ull);
+    return (r2 || rl >= C.p) ? rl - C.p : rl;
+}
+
+#define FS_C96G_MUL(RL, RH, W, P0, P1, G, SH, T, U, A, B, CC, T0, C, T1, T2, Z, Q, F, X0, X1, Y1, Y2) \
+    "mul.wide.u32 " T ", " RL ", kk;\n\t"                                        \
+    "mov.b64 {" T0 ", " C "}, " T ";\n\t"                                        \
+    "mov.b64 " CC ", {" C ", zr};\n\t"                                           \
+    "mad.wide.u32 " U ", " RH ", kk, " CC ";\n\t"                                \
+    "mov.b64 {" T1 ", " T2 "}, " U ";\n\t"                                       \
+    "mad.lo.u32 " T2 ", " W ", kk, " T2 ";\n\t"                                  \
+    "shf.r.clamp.b32 " Z ", " T1 ", " T2 ", " SH ";\n\t"                         \
+    "mov.b32 " F ", " Z ";\n\t"                                                  \
+    "fma.rm.f32 " F ", " F ", " G ", 0f00000000;\n\t"                            \
+    "mov.b32 " Q ", " F ";\n\t"                                                  \
+    "mul.wide.u32 " A ", " Q ", " P0 ";\n\t"                                     \
+    "mov.b64 {" X0 ", " X1 "}, " A ";\n\t"                                       \
+    "mov.b64 " CC ", {" X1 ", zr};\n\t"                                          \
+    "mad.wide.u32 " B ", " Q ", " P1 ", " CC ";\n\t"                             \
+    "mov.b64 {" Y1 ", " Y2 "}, " B ";\n\t"                                       \
+    "sub.cc.u32 " RL ", " T0 ", " X0 ";\n\t"                                     \
+    "subc.cc.u32 " RH ", " T1 ", " Y1 ";\n\t"                                    \
+    "subc.u32 " W ", " T2 ", " Y2 ";\n\t"
+#define FS_C96G_STEP2(J)                                                                                  \
+    "add.u32 kk, %5, " #J ";\n\t"                                                                         \
+    FS_HF_TEST("%0", "%10", "%11")                                                                        \
+    FS_HF_TEST("%2", "%16", "%17")                                                                        \
+    FS_C96G_MUL("%0", "%1", "aw", "%6", "%7", "%8", "%9", "TA", "UA", "AA", "BA", "CA", "a0", "ac", "a1", "a2", \
+                "az", "aq", "af", "ax0", "ax1", "ay1", "ay2")                                             \
+    FS_C96G_MUL("%2", "%3", "bw", "%12", "%13", "%14", "%15", "TB", "UB", "AB", "BB", "CB", "b0", "bc", "b1",   \
+                "b2", "bz", "bq", "bf", "bx0", "bx1", "by1", "by2")
+
+__device__ __forceinline__ u32 canon96g_walk8x2(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const Canon96G& A,
+                                                const Canon96G& B) {
+    u32 flag;
+    asm("{\n\t"
+        ".reg .u32 kk, zr, a0, ac, a1, a2, az, aq, ax0, ax1, ay1, ay2, aw;\n\t"
+        ".reg .u32 b0, bc, b1, b2, bz, bq, bx0, bx1, by1, by2, bw;\n\t"
+        ".reg .f32 af, bf;\n\t"
+        ".reg .u64 TA, UA, AA, BA, CA, RA, PA, TB, UB, AB, BB, CB, RB, PB;\n\t"
+        ".reg .pred P, GA, GB;\n\t"
+        "mov.u32 zr, 0;\n\t"
+        "mov.u32 aw, 0;\n\t"
+        "mov.u32 bw, 0;\n\t"
+        "mov.b64 PA, {%6, %7};\n\t"
+        "mov.b64 PB, {%12, %13};\n\t"
+        "setp.ne.u32 P, %5, %5;\n\t"
+        FS_C96G_STEP2(0) FS_C96G_STEP2(1) FS_C96G_STEP2(2) FS_C96G_STEP2(3)
+        FS_C96G_STEP2(4) FS_C96G_STEP2(5) FS_C96G_STEP2(6) FS_C96G_STEP2(7)
+        FS_C96H_FOLD("%0", "%1", "aw", "RA", "PA", "%6", "%7", "GA")
+        FS_C96H_FOLD("%2", "%3", "bw", "RB", "PB", "%12", "%13", "GB")
+        "selp.u32 %4, 1, 0, P;\n\t"
+        "}"
+        : "+r"(al), "+r"(ah), "+r"(bl), "+r"(bh), "=r"(flag)
+        : "r"(k1), "r"(A.p0), "r"(A.p1), "f"(A.g), "r"(A.sh), "r"(A.x0), "r"(A.x1),
+          "r"(B.p0), "r"(B.p1), "f"(B.g), "r"(B.sh), "r"(B.x0), "r"(B.x1));
+    return flag;
+}
+
 }  // namespace fs

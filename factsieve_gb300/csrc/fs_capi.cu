@@ -337,7 +337,8 @@ int run_sieve(fs_ctx* c, const u64* d_cand, uint32_t cap, fs::Counters* d_ctr, u
         int smode = first ? setup_mode : fs::SETUP_LOAD;
         // p = 2^63 + d, d < 2^30 over the segment: the four-candidate kernels of
         // the 96-bit walks fold their setup products instead of Montgomery's
-        if (smode == fs::SETUP_PLAN && kv == 5 && (walk == fs::WALK_C96H || walk == fs::WALK_C96) &&
+        if (smode == fs::SETUP_PLAN && kv == 5 &&
+            (walk == fs::WALK_C96H || walk == fs::WALK_C96G || walk == fs::WALK_C96) &&
             fs::pm_setup_for_range(plo, phi))
             smode = fs::SETUP_PLAN_PM;
         CK(c, fs::launch_sieve(a, smode, fin, sieve_grid(c, kv), c->stream, kv, walk, block_threads(c)));
@@ -778,8 +779,8 @@ int fs_walk_step(uint64_t plo, uint64_t phi, uint32_t kmax) { return fs::walk_fo
 int fs_setup_form(uint64_t plo, uint64_t phi) { return fs::pm_setup_for_range(plo, phi); }
 
 int fs_bench_int_pipe(fs_ctx* c, uint32_t kind, uint32_t iters, double* ops_per_sec, double* ms) {
-    if (!c || kind > 18 || iters == 0 || iters > (1u << 24)) return FS_E_ARG;
-    // kinds 16-18 walk multipliers up to 100001 + 8 iters, within their k_max bound
+    if (!c || kind > 19 || iters == 0 || iters > (1u << 24)) return FS_E_ARG;
+    // kinds 16-19 walk multipliers up to 100001 + 8 iters, within their k_max bound
     if (kind >= 16 && 100001u + 8u * iters > 1276526u) return FS_E_ARG;
     int rc = bind(c);
     if (rc) return rc;

@@ -255,7 +255,9 @@ __global__ void __launch_bounds__(256) imad_bench_kernel(u32 iters, u32 kind, u3
 //   kind 16 float-quotient steps, k_max-aware window, s >= 32 (HG: halff_walk8x2), 4 chains
 //   kind 17 the same with s <= 32 (HGL: halfgl_walk8x2), 4 chains
 //   kind 18 the same with a 96-bit t (HG96: halfg96_walk8x2), 4 chains
-constexpr u32 kCeilUnits[19] = {0, 0, 0, 0, 8, 32, 32, 32, 32, 4, 32, 32, 32, 32, 32, 8, 32, 32, 32};
+//   kind 19 half-offset 96-bit steps for p >= 2^63 with that quotient
+//           (canon96g_walk8x2), 4 chains
+constexpr u32 kCeilUnits[20] = {0, 0, 0, 0, 8, 32, 32, 32, 32, 4, 32, 32, 32, 32, 32, 8, 32, 32, 32, 32};
 
 template <u32 kind>
 __global__ void __launch_bounds__(256) ceiling_kernel(u32 iters, u32 seed, u32* sink) {
@@ -396,6 +398,14 @@ __global__ void __launch_bounds__(256) ceiling_kernel(u32 iters, u32 seed, u32* 
                 acc += canon96h_walk8x2(l[0], hh[0], l[1], hh[1], k0 + 8 * it, A, B);
                 acc += canon96h_walk8x2(l[2], hh[2], l[3], hh[3], k0 + 8 * it, C, D);
             }
+        } else if constexpr (kind == 19) {
+            const u32 kmax = k0 + 8 * iters;
+            const Canon96G A = make_canon96g(c[0], kmax), B = make_canon96g(c[1], kmax);
+            const Canon96G C = make_canon96g(c[2], kmax), D = make_canon96g(c[3], kmax);
+            for (u32 it = 0; it < iters; ++it) {
+                acc += canon96g_walk8x2(l[0], hh[0], l[1], hh[1], k0 + 8 * it, A, B);
+                acc += canon96g_walk8x2(l[2], hh[2], l[3], hh[3], k0 + 8 * it, C, D);
+            }
         } else if constexpr (kind == 10) {
             const u32 kmax = k0 + 8 * iters;
             const Half96 A = make_half96(c[0], kmax), B = make_half96(c[1], kmax);
@@ -462,12 +472,13 @@ cudaError_t launch_imad_bench(u32 iters, u32 kind, u32 seed, u32* sink, int grid
         case 16: ceiling_kernel<16><<<grid, 256, 0, s>>>(iters, seed, sink); break;
         case 17: ceiling_kernel<17><<<grid, 256, 0, s>>>(iters, seed, sink); break;
         case 18: ceiling_kernel<18><<<grid, 256, 0, s>>>(iters, seed, sink); break;
+        case 19: ceiling_kernel<19><<<grid, 256, 0, s>>>(iters, seed, sink); break;
         default: imad_bench_kernel<<<grid, 256, 0, s>>>(iters, kind, seed, sink); break;
     }
     return cudaGetLastError();
 }
 
-double bench_units_per_thread_iter(u32 kind) { return kind < 4 ? 8.0 : (kind < 19 ? kCeilUnits[kind] : 0.0); }
+double bench_units_per_thread_iter(u32 kind) { return kind < 4 ? 8.0 : (kind < 20 ? kCeilUnits[kind] : 0.0); }
 
 // bitlen(ceil(23 p kmax / 16)) - 24: the window shift of make_halfg.
 static int halfg_window_host(uint64_t p, uint32_t kmax) {
@@ -494,7 +505,7 @@ int walk_for_range(uint64_t plo, uint64_t phi, uint32_t kmax) {
     // s = bitlen(ceil(23 p kmax / 16)) - 24 on one side of 32: s <= 32 with
     // t < 2^64 (HGL), s >= 32 with t < 2^64 (HG), s in [32, 64) with p < 2^63
     // (HG96, t up to 96 bits)
-    if (plo >= (1ull << 31) && kmax <= kHalfGMaxK) {
+    if (plo >= (1ull << 31) && (pmax >> 63) == 0 && kmax <= kHalfGMaxK) {
         const int slo = halfg_window_host(plo, kmax), shi = halfg_window_host(pmax, kmax);
         const bool t64 = ((unsigned __int128)23 * pmax * kmax + 15) / 16 < ((unsigned __int128)1 << 64);
         if (t64 && shi <= 32) return WALK_HGL;
@@ -513,6 +524,8 @@ int walk_for_range(uint64_t plo, uint64_t phi, uint32_t kmax) {
     if (kb <= 26 && plo > (1ull << 33) && (pmax >> 63) == 0 && (64 - __builtin_clzll(plo)) + kb >= 61)
         return WALK_H96;
     if (kb <= 28 && plo > (1ull << 33) && (pmax >> 63) == 0) return WALK_L96;
+    // the same with the float quotient for p >= 2^63 (canon96g_ok): 46 kmax < 7 2^23
+    if ((plo >> 63) != 0 && kmax <= kHalfGMaxK) return WALK_C96G;
     // the half-offset canonical 96-bit step needs p >= 2^63 and kmax < 2^26 (canon96h_ok)
     if (kb <= 26 && (plo >> 63) != 0) return WALK_C96H;
     if (kb <= 28 && (plo >> 63) != 0) return WALK_C96;

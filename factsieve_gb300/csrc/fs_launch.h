@@ -13,7 +13,8 @@ namespace fs {
 enum { SETUP_LOAD = 0, SETUP_PLAN = 1, SETUP_PARTIALS = 2, SETUP_PLAN_PM = 3 };
 // Walk step used for every candidate of a launch (WALK_ANY: per candidate).
 enum { WALK_ANY = 0, WALK_T64 = 1, WALK_L96 = 2, WALK_C96 = 3, WALK_H64 = 4, WALK_H96 = 5, WALK_H32 = 6, WALK_HM = 7,
-       WALK_C96H = 8, WALK_HF = 9, WALK_HG = 10, WALK_HGL = 11, WALK_HG96 = 12 };
+       WALK_C96H = 8, WALK_HF = 9, WALK_HG = 10, WALK_HGL = 11, WALK_HG96 = 12,
+       WALK_C96G = 13 };
 
 // Candidate generator over the odd numbers o0 + 2 j < high.
 struct GenArgs {

@@ -120,7 +120,8 @@ extern "C" int fs_segment_noalloc(uint64_t low, uint64_t high, uint32_t nmin, ui
     const int walk = fs::walk_for_range(low, high, nmax);
     const int kv = walk == fs::WALK_ANY ? 3 : 5;
     int smode = fs::SETUP_PLAN;
-    if (kv == 5 && (walk == fs::WALK_C96H || walk == fs::WALK_C96) && fs::pm_setup_for_range(low, high))
+    if (kv == 5 && (walk == fs::WALK_C96H || walk == fs::WALK_C96G || walk == fs::WALK_C96) &&
+        fs::pm_setup_for_range(low, high))
         smode = fs::SETUP_PLAN_PM;
     const int grid = ds->sm_count * (kv == 5 ? 4 * ds->occ5 : ds->occ3);
     if (fs::launch_sieve(a, smode, true, grid, s, kv, walk) != cudaSuccess) return FS_E_CUDA;

@@ -31,6 +31,7 @@ cudaError_t launch_sieve_pair(const SieveArgs& a, int setup, bool final_chunk, i
         case WALK_H32: launch_sieve_w<3, WALK_H32>(a, setup, final_chunk, grid, s, threads); break;
         case WALK_HM: launch_sieve_w<3, WALK_HM>(a, setup, final_chunk, grid, s, threads); break;
         case WALK_C96H: launch_sieve_w<3, WALK_C96H>(a, setup, final_chunk, grid, s, threads); break;
+        case WALK_C96G: launch_sieve_w<3, WALK_C96G>(a, setup, final_chunk, grid, s, threads); break;
         case WALK_T64: launch_sieve_w<3, WALK_T64>(a, setup, final_chunk, grid, s, threads); break;
         case WALK_L96: launch_sieve_w<3, WALK_L96>(a, setup, final_chunk, grid, s, threads); break;
         case WALK_C96: launch_sieve_w<3, WALK_C96>(a, setup, final_chunk, grid, s, threads); break;

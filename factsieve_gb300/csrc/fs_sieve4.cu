@@ -6,7 +6,7 @@ namespace fs {
 
 template <int MINB, int WALK, int PPT = 2>
 static void launch_sieve_w(const SieveArgs& a, int setup, bool fin, int grid, cudaStream_t s, int t) {
-    if constexpr (WALK == WALK_C96H || WALK == WALK_C96) {
+    if constexpr (WALK == WALK_C96H || WALK == WALK_C96G || WALK == WALK_C96) {
         if (setup == SETUP_PLAN_PM) {
             if (fin) sieve_kernel<SETUP_PLAN_PM, true, MINB, WALK, PPT><<<grid, t, 0, s>>>(a);
             else sieve_kernel<SETUP_PLAN_PM, false, MINB, WALK, PPT><<<grid, t, 0, s>>>(a);
@@ -38,6 +38,7 @@ cudaError_t launch_sieve_quad(const SieveArgs& a, int setup, bool final_chunk, i
         case WALK_H32: launch_sieve_w<2, WALK_H32, 4>(a, setup, final_chunk, grid, s, threads); break;
         case WALK_HM: launch_sieve_w<2, WALK_HM, 4>(a, setup, final_chunk, grid, s, threads); break;
         case WALK_C96H: launch_sieve_w<2, WALK_C96H, 4>(a, setup, final_chunk, grid, s, threads); break;
+        case WALK_C96G: launch_sieve_w<2, WALK_C96G, 4>(a, setup, final_chunk, grid, s, threads); break;
         case WALK_T64: launch_sieve_w<2, WALK_T64, 4>(a, setup, final_chunk, grid, s, threads); break;
         case WALK_L96: launch_sieve_w<2, WALK_L96, 4>(a, setup, final_chunk, grid, s, threads); break;
         case WALK_C96: launch_sieve_w<2, WALK_C96, 4>(a, setup, final_chunk, grid, s, threads); break;

@@ -382,6 +382,18 @@ struct RegC96H {
     static __device__ __forceinline__ u64 leave(u64 r, const Prime& c, const K&) { return half_leave(r, c); }
     static __device__ __forceinline__ int hit(u64 c, const K& X) { return c == X.x ? -1 : (c == X.x + 1 ? 1 : 0); }
 };
+struct RegC96G {
+    using K = Canon96G;
+    static __device__ __forceinline__ K make(const Prime& c, u32 kmax, u64) { return make_canon96g(c, kmax); }
+    static __device__ __forceinline__ u32 block(u32& al, u32& ah, u32& bl, u32& bh, u32 k1, const K& A, const K& B) {
+        return canon96g_walk8x2(al, ah, bl, bh, k1, A, B);
+    }
+    static __device__ __forceinline__ u64 step(u64 r, u32 k, const K& X) { return canon96g_step(r, k, X); }
+    static __device__ __forceinline__ u64 canon(u64 r, const K&) { return r; }
+    static __device__ __forceinline__ u64 enter(u64 r, const Prime& c, const K& X) { return half_enter(r, c, X.x); }
+    static __device__ __forceinline__ u64 leave(u64 r, const Prime& c, const K&) { return half_leave(r, c); }
+    static __device__ __forceinline__ int hit(u64 c, const K& X) { return c == X.x ? -1 : (c == X.x + 1 ? 1 : 0); }
+};
 struct RegH96 {
     using K = Half96;
     static __device__ __forceinline__ K make(const Prime& c, u32 kmax, u64) { return make_half96(c, kmax); }
@@ -547,6 +559,7 @@ __device__ __forceinline__ void walk_pair_as(u64& ra, u64& rb, const Prime& a, c
     else if (WALK == WALK_H32) walk_reg_pair<RegH32>(ra, rb, a, b, real_b, nstart, nend, o);
     else if (WALK == WALK_HM) walk_reg_pair<RegHM>(ra, rb, a, b, real_b, nstart, nend, o);
     else if (WALK == WALK_C96H) walk_reg_pair<RegC96H>(ra, rb, a, b, real_b, nstart, nend, o);
+    else if (WALK == WALK_C96G) walk_reg_pair<RegC96G>(ra, rb, a, b, real_b, nstart, nend, o);
     else if (WALK == WALK_T64) walk_reg_pair<RegT64>(ra, rb, a, b, real_b, nstart, nend, o);
     else if (WALK == WALK_L96) walk_reg_pair<RegL96>(ra, rb, a, b, real_b, nstart, nend, o);
     else if (WALK == WALK_C96) walk_reg_pair<RegC96>(ra, rb, a, b, real_b, nstart, nend, o);
@@ -632,6 +645,7 @@ __device__ __forceinline__ void walk_quad_as(u64 (&r)[4], Prime (&c)[4], u32 nre
     else if (WALK == WALK_H32) walk_reg4<RegH32>(r, c, nreal, nstart, nend, o);
     else if (WALK == WALK_HM) walk_reg4<RegHM>(r, c, nreal, nstart, nend, o);
     else if (WALK == WALK_C96H) walk_reg4<RegC96H>(r, c, nreal, nstart, nend, o);
+    else if (WALK == WALK_C96G) walk_reg4<RegC96G>(r, c, nreal, nstart, nend, o);
     else if (WALK == WALK_T64) walk_reg4<RegT64>(r, c, nreal, nstart, nend, o);
     else if (WALK == WALK_L96) walk_reg4<RegL96>(r, c, nreal, nstart, nend, o);
     else if (WALK == WALK_C96) walk_reg4<RegC96>(r, c, nreal, nstart, nend, o);
@@ -655,6 +669,7 @@ __device__ __forceinline__ void walk_quad_rt(int walk, u64 (&r)[4], Prime (&c)[4
         case WALK_H32: walk_quad_as<WALK_H32>(r, c, nreal, nstart, nend, o); break;
         case WALK_HM: walk_quad_as<WALK_HM>(r, c, nreal, nstart, nend, o); break;
         case WALK_C96H: walk_quad_as<WALK_C96H>(r, c, nreal, nstart, nend, o); break;
+        case WALK_C96G: walk_quad_as<WALK_C96G>(r, c, nreal, nstart, nend, o); break;
         case WALK_T64: walk_quad_as<WALK_T64>(r, c, nreal, nstart, nend, o); break;
         case WALK_L96: walk_quad_as<WALK_L96>(r, c, nreal, nstart, nend, o); break;
         case WALK_C96: walk_quad_as<WALK_C96>(r, c, nreal, nstart, nend, o); break;

@@ -309,8 +309,9 @@ int fs_reset_stats(fs_ctx *ctx);
  * 13 half-offset canonical 96-bit steps, 14 half-offset 64-bit steps with
  * the quotient on the FP32 pipe, 15 folding products modulo 2^63 + d,
  * 16 / 17 / 18 the float-quotient steps with a k_max-aware window (window
- * shift at least 32 / at most 32 / a 96-bit product).
- * iters in [1, 2^24]; for kinds 16-18 at most 147065, so that the
+ * shift at least 32 / at most 32 / a 96-bit product), 19 the half-offset
+ * 96-bit step for p >= 2^63 with that quotient.
+ * iters in [1, 2^24]; for kinds 16-19 at most 147065, so that the
  * multipliers stay within those steps' bound 46 k_max < 7 2^23. */
 int fs_bench_int_pipe(fs_ctx *ctx, uint32_t kind, uint32_t iters, double *ops_per_sec, double *ms);
 
@@ -319,7 +320,8 @@ int fs_bench_int_pipe(fs_ctx *ctx, uint32_t kind, uint32_t iters, double *ops_pe
  * 64-bit with the quotient on the FP32 pipe / lazy 64-bit / lazy 96-bit /
  * canonical 96-bit, 10 / 11 / 12 half-offset with the FP32 quotient and a
  * window taken from kmax (64-bit product, window shift >= 32 / <= 32;
- * 96-bit product), 1 lazy 64-bit, 2 lazy 96-bit,
+ * 96-bit product), 13 the half-offset canonical 96-bit step for p >= 2^63
+ * with that quotient, 1 lazy 64-bit, 2 lazy 96-bit,
  * 3 canonical 96-bit, 0 chosen per candidate (mixed ranges, or multipliers
  * beyond the forms' limits: generic Montgomery).
  * No counterpart in the reference, whose one step is the Montgomery product. */

@@ -116,16 +116,16 @@ def test_plan_check_flags_a_corrupted_plan(ctx, what):
 
 
 def test_ceiling_kernels_report_rates(ctx):
-    """The roofline's ceiling microkernels (fs_bench_int_pipe kinds 0-18) run and
+    """The roofline's ceiling microkernels (fs_bench_int_pipe kinds 0-19) run and
     report plausible rates; an unknown kind is refused, and so are iterations
-    that would take the k_max-window float-quotient kinds (16-18) past their
+    that would take the k_max-window float-quotient kinds (16-19) past their
     multiplier bound."""
     import factsieve_gb300 as fs
-    rates = {k: ctx.bench_int_pipe(k, 200)[0] for k in range(19)}
+    rates = {k: ctx.bench_int_pipe(k, 200)[0] for k in range(20)}
     assert all(v > 0 for v in rates.values()), rates
     assert rates[0] > rates[4]             # an IMAD issues faster than a Montgomery product completes
     with pytest.raises(fs.FSError):
-        ctx.bench_int_pipe(19, 200)
+        ctx.bench_int_pipe(20, 200)
     with pytest.raises(fs.FSError):
         ctx.bench_int_pipe(5, 0)
     ctx.bench_int_pipe(17, 147_065)        # multipliers up to 100,001 + 8 x 147,065 = 1,276,521

@@ -96,7 +96,8 @@ SPLIT_REGIMES = [
     (10**15, 10**15 + 200_000, 100_000, 100_700),                  # float quotient, 96-bit product
     (10**15, 10**15 + 200_000, 1_276_000, 1_277_000),              # ... into the half-offset 96-bit step at its k_max bound
     (10**13, 10**13 + 30_000, 67_108_000, 67_109_700),             # half-offset 96-bit into lazy 96-bit at 2^26
-    ((1 << 63) + 1, (1 << 63) + 200_000, 5_000, 5_700),             # half-offset canonical 96-bit
+    ((1 << 63) + 1, (1 << 63) + 200_000, 5_000, 5_700),             # half-offset canonical 96-bit, float quotient
+    ((1 << 63) + 1, (1 << 63) + 20_001, 1_276_000, 1_277_000),      # ... into the integer quotient at its k_max bound
     ((1 << 63) + 1, (1 << 63) + 10_001, (1 << 26) - 300, (1 << 26) + 400),  # into canonical 96-bit at 2^26
     ((1 << 64) - 200_000, (1 << 64) - 1, 1_000, 1_333),              # near 2^64
     (10**12, 10**12 + 200_000, 100_000, 100_700),                  # float quotient, window from the least p

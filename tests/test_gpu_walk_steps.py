@@ -31,7 +31,8 @@ STEPS = {
     1: (33, 35, 1 << 25, (1 << 26) - 1, "lazy 64-bit"),
     5: (42, 62, KB + 1, (1 << 26) - 1, "half-offset lazy 96-bit"),
     2: (34, 62, 1 << 26, (1 << 26) + (1 << 16), "lazy 96-bit"),
-    8: (63, 63, 34, 1 << 21, "half-offset canonical 96-bit"),
+    13: (63, 63, 34, KB, "half-offset canonical 96-bit, float quotient"),
+    8: (63, 63, KB + 1, (1 << 26) - 1, "half-offset canonical 96-bit"),
     3: (63, 63, 1 << 26, (1 << 26) + (1 << 16), "canonical 96-bit"),
 }
 
@@ -41,11 +42,13 @@ def _edges(step, kmax):
     out = []
     if step in (10, 12):
         out.append(((1 << 68) - 1) // (23 * kmax))          # ceil(23 p k_max / 16) reaches 2^64
+    if step in (12, 13):
+        out.append(1 << 63)                                  # the float quotient's two 96-bit forms meet
     if step in (10, 11):
         out += [((1 << 56) * 16) // (23 * kmax), ((1 << 55) * 16) // (23 * kmax)]   # window shift 32
     if step in (4, 1):
         out.append((1 << 62) // kmax)                        # p k_max = 2^62
-    return [e for e in out if (1 << 31) < e < (1 << 63)]
+    return [e for e in out if (1 << 31) < e <= (1 << 63)]
 
 
 def _cases(step, count, seed):

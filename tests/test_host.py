@@ -178,11 +178,12 @@ def test_context_needs_a_device(fslib):
 def test_walk_step_selection_boundaries(fslib):
     """The launch-wide step the host proves valid for a p-segment (fs_walk_step)."""
     H64, T64, L96, C96, H96, H32, HM, C96H, HF, ANY = 4, 1, 2, 3, 5, 6, 7, 8, 9, 0
-    HG, HGL, HG96 = 10, 11, 12
+    HG, HGL, HG96, C96G = 10, 11, 12, 13
     ws = fslib.walk_step
     assert ws(10**12, 10**12 + 10**8, 200_000) == HF                       # config 2
     assert ws(10**12, 10**12 + 10**9, 200_000) == HF                       # config 2, whole range
-    assert ws(1 << 63, (1 << 63) + 10**9, 1_010_000) == C96H               # config 3
+    assert ws(1 << 63, (1 << 63) + 10**9, 1_010_000) == C96G               # config 3: float quotient
+    assert ws(1 << 63, (1 << 63) + 10**9, 1_276_527) == C96H               # past its k_max bound
     assert ws(1 << 63, (1 << 63) + 10**9, 1 << 26) == C96                   # k_max >= 2^26 at p >= 2^63
     assert ws(10**6, 2 * 10**6, 2000) == H32                               # config 1: p < 2^31
     assert ws(127, 100_000, 1_000_000) == H32                              # self test 3 (p <= nmax)
@@ -215,7 +216,8 @@ def test_walk_step_selection_boundaries(fslib):
     edge = ((1 << 68) - 1) // (23 * kb)                                     # last pmax with ceil(23 pmax kb / 16) < 2^64
     assert ws(edge - 1000, edge + 1, kb) == HG and ws(edge - 1000, edge + 2, kb) == HG96
     assert ws((1 << 63) - 10**6, (1 << 63) - 1, kb) == HG96 and ws((1 << 63) - 10**6, 1 << 63, kb) == HG96
-    assert ws(1 << 63, (1 << 63) + 10**6, 1000) == C96H                     # p >= 2^63: no float-quotient step
+    assert ws(1 << 63, (1 << 63) + 10**6, 1000) == C96G                     # p >= 2^63: the 96-bit canonical form
+    assert ws((1 << 64) - 10**6, (1 << 64) - 1, kb) == C96G
     # the window shift on one side of 32: HGL while T = ceil(23 pmax k_max / 16) < 2^56
     # (s <= 32), HG while T(plo) >= 2^55 (s >= 32), neither across both
     T = lambda p: (23 * p * kb + 15) // 16
@@ -397,6 +399,50 @@ def test_kmax_window_float_quotient_holds_where_the_host_selects_it(fslib):
             r = r2
     # beyond the k_max bound the steps are not chosen
     assert fslib.walk_step((1 << 40) + 1, (1 << 40) + 1001, 1_276_527) not in (10, 11, 12)
+
+
+def _c96g_step(r, k, p, kmax):
+    """Word-level restatement of the float-quotient step for p >= 2^63
+    (canon96g_walk8x2, fs_arith.cuh) on a lazy residue of up to 65 bits:
+    t = r k, s = bitlen(ceil(23 p kmax / 16)) - 24, z = t >> s read as the
+    subnormal z 2^-149, one round-down fma by g = m 2^(s-87), m = floor(2^87 / p);
+    r' = t - q p, exact."""
+    from fractions import Fraction
+    assert p >> 63
+    T = (23 * p * kmax + 15) // 16
+    s = T.bit_length() - 24
+    assert 32 <= s < 64
+    m = (1 << 87) // p
+    assert (1 << 23) <= m < (1 << 24)
+    g = _f32(((s - 87 + 149) << 23) + m)
+    assert g == Fraction(m, 1 << (87 - s))
+    t = r * k
+    assert t < 1 << 96
+    z = t >> s
+    assert z < 1 << 24 and z == ((t >> 32) >> (s - 32)) & 0xFFFFFFFF    # the funnel shift of t's upper words
+    q = int(_f32(z) * g * (1 << 149))
+    assert q <= t // p
+    return t - q * p
+
+
+def test_float_quotient_for_p_above_2_63_keeps_its_bound(fslib):
+    """Wherever fs_walk_step picks the float-quotient 96-bit step for p >= 2^63
+    (13), each step is exact, never negative, and keeps the lazy residue below
+    (23/16) p (65 bits) over the last multipliers up to k_max, at the bound."""
+    import random
+    rng = random.Random(13)
+    for _ in range(40):
+        lo = rng.choice([(1 << 63) + rng.randrange(1, 1 << 30), rng.randrange(1 << 63, (1 << 64) - 10**6),
+                         (1 << 64) - rng.randrange(10**6, 10**7)])
+        kmax = rng.choice([1_276_526, rng.randrange(2, 1_276_527), rng.randrange(1_000_000, 1_276_527)])
+        hi = lo + 1000
+        assert fslib.walk_step(lo, hi, kmax) == 13
+        for p in ((lo | 1), (hi - 2) | 1):
+            r = p - 1
+            for k in range(max(1, kmax - 120), kmax + 1):
+                r2 = _c96g_step(r, k, p, kmax)
+                assert r2 >= 0 and r2 % p == (r * k) % p and 16 * r2 < 23 * p
+                r = r2
 
 
 def _pm_mul(a, b, p):
