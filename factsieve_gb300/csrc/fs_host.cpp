@@ -114,11 +114,6 @@ static void pack_layer(const std::vector<uint32_t>& v, std::vector<uint64_t>& wo
         upto[x] = i;
     }
     const uint64_t vmax = v[m - 1];
-    auto slots_upto = [&](uint64_t x) -> uint32_t {
-        if (x >= vmax) return m;
-        if (x < kSmall) return upto[x];
-        return (uint32_t)(std::upper_bound(v.begin(), v.end(), x) - v.begin());
-    };
     auto find = [&below](uint32_t x) {
         while (below[x] != x) {
             below[x] = below[below[x]];
@@ -126,11 +121,26 @@ static void pack_layer(const std::vector<uint32_t>& v, std::vector<uint64_t>& wo
         }
         return x;
     };
-    for (uint32_t top = find(m); top != 0; top = find(top)) {
+    // the largest slot left: slots go mostly from the top, so a cursor that
+    // only moves down finds it without the union-find
+    uint32_t hi = m;
+    auto top_left = [&below, &hi]() {
+        while (hi != 0 && below[hi] != hi) --hi;
+        return hi;
+    };
+    // the largest slot left whose prime fits beside w (one 64-bit division
+    // only when even the largest prime does not)
+    auto largest_fit = [&](uint64_t w) -> uint32_t {
+        if ((u128)w * vmax <= (u128)UINT64_MAX) return top_left();
+        const uint64_t x = UINT64_MAX / w;
+        if (x < kSmall) return find(upto[x]);
+        return find((uint32_t)(std::upper_bound(v.begin(), v.end(), x) - v.begin()));
+    };
+    for (uint32_t top = top_left(); top != 0; top = top_left()) {
         uint64_t w = v[top - 1];
         below[top] = top - 1;
         for (;;) {
-            const uint32_t s = find(slots_upto(UINT64_MAX / w));
+            const uint32_t s = largest_fit(w);
             if (s == 0) break;
             w *= v[s - 1];
             below[s] = s - 1;
